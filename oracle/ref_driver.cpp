@@ -1,0 +1,108 @@
+/*
+ * Driver for the REFERENCE sampler, compiled unmodified from its own headers
+ * (MarcJos/RSA_MPI include/) against the single-rank MPI stand-in in
+ * oracle/mpi_standin/.  TEST INFRASTRUCTURE ONLY: its outputs pin the oracle
+ * restatement (oracle/rsa_oracle.c) and produce the committed golden fixtures.
+ *
+ * Usage:
+ *   ref_rsa run <dim> <seed> <nbshots> <volume_mode> <L_0..L_{D-1}> <k> (<r> <phi> <phase>)*k  <out.bin>
+ *
+ *   volume_mode: 0 -> RadiusGenerator volume = total box volume
+ *                     (rsa_algo::uniform_generate, operator_algorithm.ixx:507-515)
+ *                1 -> volume = 1 (the quirk of ::throw_spheres, test.hxx:21)
+ *
+ * Runs algorithm::uniform_generate<DIM, 1, true> (operator_algorithm.ixx:517-524)
+ * on the periodic box [0, L] with ghost layer 1 and domain radius = r_max, the
+ * same call chain as ::throw_spheres (test.hxx:13-32).  The plog=true template
+ * argument makes the reference print its per-round trace (miss rate, shots,
+ * voxels) on stdout.  The final spheres are written to <out.bin>:
+ *   int32 dim, int64 n, then n records of {double center[dim], double radius, int32 phase}.
+ * The wall time of proceed() alone is printed as "proceed_seconds <t>".
+ */
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include <rsa_domain.hxx>
+#include <radius_generator.hxx>
+#include <operator_algorithm.hxx>
+
+namespace {
+
+template<int DIM>
+int run(int argc, char** argv) {
+    // argv: run dim seed nbshots volume_mode L... k (r phi phase)* out
+    int a = 2;
+    size_t seed = std::strtoull(argv[a++], nullptr, 10);
+    int nbshots = std::atoi(argv[a++]);
+    int volume_mode = std::atoi(argv[a++]);
+    std::array<double, DIM> inf{}, sup{};
+    for (int d = 0; d < DIM; d++) {
+        inf[d] = 0.;
+        sup[d] = std::strtod(argv[a++], nullptr);
+    }
+    int k = std::atoi(argv[a++]);
+    std::vector<std::tuple<double, double, int>> classes;
+    for (int i = 0; i < k; i++) {
+        double r = std::strtod(argv[a++], nullptr);
+        double phi = std::strtod(argv[a++], nullptr);
+        int ph = std::atoi(argv[a++]);
+        classes.emplace_back(r, phi, ph);
+    }
+    std::string out = argv[a++];
+    if (a > argc) return 2;
+
+    double volume = 1.;
+    for (int d = 0; d < DIM; d++) volume *= (sup[d] - inf[d]);
+    if (volume_mode == 1) volume = 1.;
+    sac_de_billes::RadiusGenerator<DIM> radius_generator(classes, volume);
+    rsa_domain<DIM> domain(inf, sup, 1, radius_generator.get_max_radius());
+
+    auto t0 = std::chrono::steady_clock::now();
+    algorithm::uniform_generate<DIM, 1, true>(domain, radius_generator, nbshots, 10, seed);
+    auto t1 = std::chrono::steady_clock::now();
+    std::printf("proceed_seconds %.6f\n", std::chrono::duration<double>(t1 - t0).count());
+
+    auto spheres = domain.extract_spheres();
+    FILE* f = std::fopen(out.c_str(), "wb");
+    if (!f) return 3;
+    int32_t dim = DIM;
+    int64_t n = spheres.size();
+    std::fwrite(&dim, sizeof(dim), 1, f);
+    std::fwrite(&n, sizeof(n), 1, f);
+    for (const auto& s : spheres) {
+        std::fwrite(s.center.data(), sizeof(double), DIM, f);
+        double r = s.radius;
+        int32_t ph = s.phase;
+        std::fwrite(&r, sizeof(r), 1, f);
+        std::fwrite(&ph, sizeof(ph), 1, f);
+    }
+    std::fclose(f);
+    std::printf("spheres %lld volume_of_spheres %.17g\n", (long long)n,
+        domain.compute_total_volume_of_spheres());
+    return 0;
+}
+
+} // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 3 || std::string(argv[1]) != "run") {
+        std::fprintf(stderr, "usage: ref_rsa run <dim> <seed> <nbshots> <volume_mode> <L...> <k> (<r> <phi> <phase>)* <out>\n");
+        return 2;
+    }
+    int dim = std::atoi(argv[2]);
+    // shift argv so that argv[2] is the seed
+    argv[2] = argv[1];
+    argv++;
+    argc--;
+    switch (dim) {
+    case 2: return run<2>(argc, argv);
+    case 3: return run<3>(argc, argv);
+    case 4: return run<4>(argc, argv);
+    default:
+        std::fprintf(stderr, "dim %d not built\n", dim);
+        return 2;
+    }
+}
