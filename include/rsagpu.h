@@ -1,0 +1,187 @@
+/*
+ * rsagpu.h -- C ABI of the GB300 sampler (bias-free maximal Poisson-sphere
+ * sampling by random sequential addition with voxel subdivision).
+ *
+ * Plain C types only: opaque handles, pointers to host buffers and sizes.
+ * Every function returns RSAGPU_OK (0) or a negative status; the text of the
+ * last error of the calling thread is returned by rsagpu_last_error().
+ *
+ * Each entry point names the reference interface it replaces
+ * (MarcJos/RSA_MPI, file:line).  The reference is header-only C++; its Python
+ * binding (Interface_python/Interface.cxx) is replaced by the ctypes module
+ * rsa_mpi_gb300.rsa_mpi_py, and its C++ facade by include/rsa_gpu/user_interface.hxx.
+ *
+ * Threading: one CUDA stream per algo handle.  Calls on one handle are not
+ * thread-safe; calls on different handles are.  All device memory of a
+ * domain lives on the GPU that was current when the domain was created.
+ */
+#ifndef RSAGPU_H
+#define RSAGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RSAGPU_MAX_DIM 7
+
+/* status codes */
+#define RSAGPU_OK 0
+#define RSAGPU_ERR_ARG (-1)          /* invalid argument (std::runtime_error in the reference) */
+#define RSAGPU_ERR_CUDA (-2)         /* CUDA runtime failure (allocation, launch) */
+#define RSAGPU_ERR_NO_PROGRESS (-3)  /* a device loop hit its iteration cap */
+#define RSAGPU_ERR_STATE (-4)        /* call out of order (e.g. refine before begin) */
+#define RSAGPU_ERR_INVARIANT (-5)    /* a device check failed (two centres in one cell, ...) */
+#define RSAGPU_ERR_PIVOT (-6)        /* count-cap pivot search failed (the reference throws here) */
+#define RSAGPU_ERR_CAPACITY (-7)     /* a size limit of this build was exceeded */
+
+typedef struct rsagpu_domain rsagpu_domain;
+typedef struct rsagpu_radgen rsagpu_radgen;
+typedef struct rsagpu_algo rsagpu_algo;
+
+const char* rsagpu_last_error(void);
+/* Library version string. */
+const char* rsagpu_version(void);
+/* Number of CUDA kernels this process launched through the library (for accounting). */
+uint64_t rsagpu_kernel_launches(void);
+
+/* ---- domain: replaces ::rsa_domain<DIM> / user_interface::rsa_domain<DIM>
+ *      (include/rsa_domain.hxx:18-94, include/user_interface.hxx:13-53).
+ * The periodic box [inf, sup]; rad_max bounds the radius of every sphere placed in it
+ * (the reference's cell size / ghost width, rsa_domain.ixx:6-28). */
+int rsagpu_domain_create(int dim, const double* inf, const double* sup, double rad_max,
+                         rsagpu_domain** out);
+int rsagpu_domain_destroy(rsagpu_domain* dom);
+/* get_total_volume (rsa_domain.ixx:164-168) */
+int rsagpu_domain_total_volume(const rsagpu_domain* dom, double* out);
+/* compute_total_volume_of_spheres (rsa_domain.ixx:170-175) */
+int rsagpu_domain_spheres_volume(rsagpu_domain* dom, double* out);
+/* number of spheres placed (rsa_grid::get_number_of_spheres_fast, rsa_grid.hxx:64) */
+int rsagpu_domain_count(rsagpu_domain* dom, uint64_t* out);
+/* extract_spheres (rsa_grid.ixx:88-98): copies at most cap spheres into caller buffers
+ * (centers: cap*dim doubles, row major; radii: cap; phases: cap; any may be NULL) in cell order,
+ * and writes the number of spheres to *n_out. */
+int rsagpu_domain_extract(rsagpu_domain* dom, double* centers, double* radii, int* phases,
+                          uint64_t cap, uint64_t* n_out);
+/* operator_check_cell validators (operator_check_cell.ixx:8-78, rsa_data_storage.ixx:216-243):
+ * number of overlapping pairs (exact FP64, periodic images) and of spheres stored in a cell that
+ * does not contain their centre. */
+int rsagpu_domain_check(rsagpu_domain* dom, uint64_t* overlapping_pairs, uint64_t* misplaced);
+
+/* ---- radius generator: replaces sac_de_billes::RadiusGenerator<DIM>
+ *      (include/radius_generator.hxx:46-105, radius_generator.ixx:9-86). */
+/* (radius, count, phase) classes; placed by nonincreasing radius. */
+int rsagpu_radgen_create_counts(int dim, const double* radii, const uint64_t* counts,
+                                const int* phases, int n_classes, double exclusion_distance,
+                                rsagpu_radgen** out);
+/* (radius, volume fraction, phase) classes: count = uint64(volume * phi / v_D(r)). */
+int rsagpu_radgen_create_fractions(int dim, const double* radii, const double* fractions,
+                                   const int* phases, int n_classes, double volume,
+                                   double exclusion_distance, rsagpu_radgen** out);
+int rsagpu_radgen_destroy(rsagpu_radgen* rg);
+int rsagpu_radgen_max_radius(const rsagpu_radgen* rg, double* out);
+int rsagpu_radgen_min_radius(const rsagpu_radgen* rg, double* out);
+
+/* ---- algorithm: replaces algorithm::rsa_algo<DIM> / user_interface::rsa_algo<DIM>
+ *      (include/operator_algorithm.hxx:18-109, include/user_interface.hxx:85-110).
+ * The algo keeps a reference to the domain (which must outlive it) and a copy of the
+ * radius generator.  Creating it clears the spheres of the domain (operator_algorithm.ixx:15-30). */
+int rsagpu_algo_create(rsagpu_domain* dom, const rsagpu_radgen* rg, int nbshots,
+                       rsagpu_algo** out);
+int rsagpu_algo_destroy(rsagpu_algo* algo);
+
+/* precision form */
+#define RSAGPU_FORM_FP64 0        /* every decision in FP64 */
+#define RSAGPU_FORM_FP32_GUARD 1  /* FP32 decisions outside a guard band, FP64 inside it */
+/* schedule of darts and subdivisions */
+#define RSAGPU_SCHEDULE_HEURISTIC 0 /* darts per round from the voxel count, refine on miss rate */
+#define RSAGPU_SCHEDULE_LEARNED 1   /* MLP decides when to refine (heuristic as fallback) */
+#define RSAGPU_SCHEDULE_REFERENCE 2 /* the reference's round sizes: Poisson(min(nbshots, 0.01 V)) */
+int rsagpu_algo_set_form(rsagpu_algo* algo, int form, int schedule);
+/* count cap of a round that would exceed the class count */
+#define RSAGPU_CAP_REFERENCE 0    /* retain_only_first_elements pivot rule (operator_algorithm.ixx:475-519) */
+#define RSAGPU_CAP_EXACT 1        /* exactly the remaining count, smallest priorities first */
+int rsagpu_algo_set_cap_rule(rsagpu_algo* algo, int rule);
+/* darts per round of the heuristic schedule = clamp(factor * voxels, min_darts, max_darts),
+ * refinement when the round's miss rate exceeds miss_threshold (<= 0: the reference's rule,
+ * operator_algorithm.ixx:344-351). */
+int rsagpu_algo_set_schedule_params(rsagpu_algo* algo, double factor, uint64_t min_darts,
+                                    uint64_t max_darts, double miss_threshold);
+/* Learned schedule: weights of the 16-64-64-2 MLP (bf16 bit patterns, row major W1[64][16], b1[64],
+ * W2[64][64], b2[64], W3[2][64], b3[2]; 16*64+64+64*64+64+2*64+2 = 5378 values). */
+int rsagpu_algo_set_mlp(rsagpu_algo* algo, const uint16_t* weights_bf16, uint64_t n);
+
+/* proceed(seed) (operator_algorithm.ixx:225-236, user_interface.hxx:101): runs rounds until no
+ * voxel is left (certified maximal) or the class list is exhausted. */
+int rsagpu_algo_proceed(rsagpu_algo* algo, uint64_t seed);
+/* reset_radius_generator (operator_algorithm.ixx:238-250): keeps the placed spheres; the new
+ * generator's largest radius may not exceed the current one. */
+int rsagpu_algo_reset_radgen(rsagpu_algo* algo, const rsagpu_radgen* rg);
+
+/* Per-round trace of the last proceed(): for each round the voxels before it, darts, accepted
+ * spheres, refinement flag (1) and voxel level; returns the number of rounds in *n_out. */
+int rsagpu_algo_trace(rsagpu_algo* algo, uint64_t* voxels, uint64_t* darts, uint64_t* accepted,
+                      uint8_t* refined, int32_t* level, uint64_t cap, uint64_t* n_out);
+/* Statistics of the last proceed(): rounds, refinements, darts, settle iterations, guard-band
+ * retests, device milliseconds per kernel family (darts, probe, settle, commit, refine). */
+typedef struct {
+    uint64_t rounds, refinements, darts, accepted, settle_iterations, retests, peak_voxels;
+    uint64_t bytes_darts, bytes_probe, bytes_settle, bytes_commit, bytes_refine;
+    double ms_darts, ms_probe, ms_settle, ms_commit, ms_refine, ms_total;
+    int32_t final_level, maximal;
+} rsagpu_stats;
+int rsagpu_algo_stats(rsagpu_algo* algo, rsagpu_stats* out);
+/* Turns per-kernel CUDA-event timing on (1) or off (0, default). */
+int rsagpu_algo_set_timing(rsagpu_algo* algo, int on);
+
+/* ---- replay seam (operator_algorithm.ixx:534-566 generate_spheres with injected candidate
+ * generators; list_of_voxels.ixx:30-100).  Used to prove decision parity with the FP64 oracle. */
+/* Builds the level-0 voxel list (list_of_voxels.ixx:11-28) and resets the round state. */
+int rsagpu_algo_begin(rsagpu_algo* algo);
+/* Decides n candidates (host arrays) against the placed spheres and among themselves, as one round
+ * of generate_spheres; keys are priorities (smaller first, equal keys do not block each other).
+ * accepted_out[i] = 1 for accepted candidates, *n_new = their number. */
+int rsagpu_algo_replay_round(rsagpu_algo* algo, uint64_t n, const double* pos, const uint64_t* key,
+                             const double* rad, const int* phase, uint64_t max_new,
+                             int may_outreach, uint8_t* accepted_out, uint64_t* n_new);
+/* Class bookkeeping and the miss-rate rule after a round (operator_algorithm.ixx:140-162);
+ * *refined = 1 if the voxels were culled and subdivided, *done = 1 if no class is left. */
+int rsagpu_algo_end_round(rsagpu_algo* algo, uint64_t n_shots, uint64_t n_new, int* refined,
+                          int* done);
+/* remove_covered + subdivide_uncovered, unconditionally (operator_algorithm.ixx:190-206). */
+int rsagpu_algo_refine(rsagpu_algo* algo);
+/* Current voxel list: count, level and length; coords (count*dim int64) may be NULL. */
+int rsagpu_algo_voxels(rsagpu_algo* algo, int64_t* coords, uint64_t cap, uint64_t* count,
+                       int32_t* level, double* length);
+/* Draws one round of darts with the product's Philox stream (round r of seed) and copies the
+ * candidates to host buffers (for checking the dart kernel); *n = number drawn. */
+int rsagpu_algo_draw_darts(rsagpu_algo* algo, uint64_t seed, uint64_t round, uint64_t n,
+                           double* pos, uint64_t* key, uint64_t* voxel_index);
+
+/* ---- batch: many independent instances in one persistent launch sequence. */
+typedef struct {
+    int dim;
+    double sup[RSAGPU_MAX_DIM];  /* box [0, sup] */
+    double radius;               /* monodisperse radius */
+    uint64_t seed;
+} rsagpu_instance_desc;
+/* Runs every instance to certified maximality; counts_out[i] = spheres of instance i.
+ * fractions_out (may be NULL) = packing fraction of each instance. */
+int rsagpu_batch_run(const rsagpu_instance_desc* inst, int n, uint64_t* counts_out,
+                     double* fractions_out, double* seconds_out);
+
+/* ---- learned schedule: MLP kernels (16-64-64-2, bf16 weights, fp32 accumulate) ---- */
+/* forward: x[n][16] (fp32) -> y[n][2] (fp32), weights as rsagpu_algo_set_mlp */
+int rsagpu_mlp_forward(const uint16_t* weights_bf16, const float* x, uint64_t n, float* y);
+/* one training step of mean squared error on (x, target): returns the loss and the gradient of every
+ * weight (fp32, same layout), and applies SGD with learning rate lr to the master fp32 weights
+ * (in/out), refreshing weights_bf16. */
+int rsagpu_mlp_train_step(float* master_weights, uint16_t* weights_bf16, const float* x,
+                          const float* target, uint64_t n, float lr, float* loss_out,
+                          float* grad_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,78 @@
+"""Builds the sampler's shared library rsa_mpi_gb300/_build/librsagpu.so with nvcc for sm_103a.
+
+The kernels are compiled once per space dimension (kernels.cu with -DRSA_DIM=2..7) in parallel,
+then linked with the dimension-independent kernels and the host driver into one shared library
+whose C ABI is include/rsagpu.h.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "librsagpu.so")
+DIMS = (2, 3, 4, 5, 6, 7)
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -fmad=false: no multiply-add contraction anywhere; the FP64 decisions also use explicit _rn intrinsics.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         f"-I{os.path.join(ROOT, 'include')}"]
+
+
+def nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return cand
+
+
+def _sources():
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))] + [
+        os.path.join(ROOT, "include", "rsagpu.h")]
+
+
+def up_to_date() -> bool:
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(s) <= t for s in _sources())
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    if not force and up_to_date():
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    jobs = []
+    for d in DIMS:
+        jobs.append(([nvcc(), *ARCH, *FLAGS, f"-DRSA_DIM={d}", "-c", os.path.join(CSRC, "kernels.cu"),
+                      "-o", os.path.join(OUT, f"kernels_d{d}.o")], f"kernels_d{d}"))
+    for name in ("kernels_common", "rsagpu"):
+        jobs.append(([nvcc(), *ARCH, *FLAGS, "-c", os.path.join(CSRC, f"{name}.cu"),
+                      "-o", os.path.join(OUT, f"{name}.o")], name))
+
+    def run(job):
+        cmd, name = job
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {name}:\n{r.stderr}")
+        if verbose and r.stderr:
+            sys.stderr.write(r.stderr)
+        return name
+
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        list(ex.map(run, jobs))
+    objs = [os.path.join(OUT, f"kernels_d{d}.o") for d in DIMS]
+    objs += [os.path.join(OUT, "kernels_common.o"), os.path.join(OUT, "rsagpu.o")]
+    tmp = LIB + ".tmp"
+    r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,658 @@
+// kernels.cu -- the sampler's kernels for one space dimension, compiled with -DRSA_DIM=D.
+//
+// One round (generate_spheres, operator_algorithm.ixx:534-566) is
+//   k_darts -> k_probe -> k_collect -> k_settle x iterations -> [count cap] -> k_commit
+// and one refinement (update_covered_voxels, :190-206) is
+//   k_refine_mask -> scan of block counts -> k_refine_write.
+#include <cfloat>
+
+#include "rsa_device.cuh"
+#include "rsa_ops.h"
+
+#ifndef RSA_DIM
+#error "compile with -DRSA_DIM=<dimension>"
+#endif
+
+namespace rsagpu {
+namespace {
+
+constexpr int D = RSA_DIM;
+constexpr int CHILDREN = 1 << D;
+constexpr int MASK_WORDS = (CHILDREN + 31) / 32;
+constexpr int K_PRE = 16;  // prefilter spheres kept in registers per parent voxel
+
+// Child order of subdivide_uncovered: TabCorner (auxiliary/Path.ixx:86-103) for D = 2, 3; for D >= 4
+// bit d of the child index is the offset along dimension d (the reference's generic table,
+// Path.ixx:105-114, writes out of bounds and never sets dimension 0).
+__device__ __forceinline__ int corner_bit(int t, int d) {
+    if (D == 2) {
+        const int tab = 0b01101100;  // (0,0) (1,1) (0,1) (1,0): bit (2t + d)
+        return (tab >> (2 * t + d)) & 1;
+    } else if (D == 3) {
+        // (0,0,0) (1,1,1) (0,0,1) (1,1,0) (0,1,0) (1,0,1) (0,1,1) (1,0,0)
+        const uint32_t tab = (0u) | (7u << 3) | (4u << 6) | (3u << 9) | (2u << 12) | (5u << 15) | (6u << 18) | (1u << 21);
+        return (tab >> (3 * t + d)) & 1;
+    } else {
+        return (t >> d) & 1;
+    }
+}
+
+__host__ __device__ inline Grid<D> make_grid(const GridArgs& a) {
+    Grid<D> g;
+    g.ncells = a.ncells;
+    for (int d = 0; d < D; d++) {
+        g.n[d] = a.n[d];
+        g.inv_c[d] = a.inv_c[d];
+    }
+    g.occ = a.occ;
+    g.pos = a.pos;
+    g.rad = a.rad;
+    g.phase = a.phase;
+    g.stencil = a.stencil;
+    g.S = a.S;
+    return g;
+}
+
+__host__ __device__ inline Geo<D> make_geo(const GridArgs& a) {
+    Geo<D> g;
+    for (int d = 0; d < D; d++) {
+        g.inf[d] = a.inf[d];
+        g.L[d] = a.L[d];
+    }
+    return g;
+}
+
+inline unsigned nblocks(uint64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+// ------------------------------------------------------------------------------------------------
+// level-0 voxel list, dimension 0 fastest (getAllIndices, auxiliary/Loops.ixx:45-69)
+// ------------------------------------------------------------------------------------------------
+struct NVox {
+    int64_t n[D];
+};
+
+__global__ void k_vox_init(int32_t* vox, uint64_t V, NVox nv) {
+    const uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    uint64_t r = v;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        vox[v * D + d] = (int32_t)(r % (uint64_t)nv.n[d]);
+        r /= (uint64_t)nv.n[d];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// darts: voxel ~ U{0..V-1}, x_d = (inf_d + coord_d len_d) + len_d u_d (pick_points,
+// list_of_voxels.ixx:107-129), priority = 32 random bits (generate_priority, operator_algorithm.ixx:373-381)
+// ------------------------------------------------------------------------------------------------
+struct DartParams {
+    uint32_t n;
+    uint64_t V;
+    const int32_t* vox;
+    double len[D];
+    double inf[D];
+    uint32_t seed_lo, seed_hi, round_lo, round_hi;
+    double radius;
+    int32_t phase;
+    double* pos;
+    uint64_t* key;
+    double* rad;
+    int32_t* cphase;
+    uint8_t* state;
+    uint64_t* vidx_out;
+};
+
+__global__ void k_darts(DartParams p) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    constexpr int WORDS = 2 + 2 * D + 1;
+    constexpr int CALLS = (WORDS + 3) / 4;
+    uint32_t w[CALLS * 4];
+    const uint2 k = make_uint2(p.seed_lo, p.seed_hi);
+#pragma unroll
+    for (int c = 0; c < CALLS; c++) {
+        const uint4 r = philox4x32_10(make_uint4(i, p.round_lo, p.round_hi, (uint32_t)c), k);
+        w[4 * c + 0] = r.x;
+        w[4 * c + 1] = r.y;
+        w[4 * c + 2] = r.z;
+        w[4 * c + 3] = r.w;
+    }
+    const uint64_t r64 = ((uint64_t)w[0] << 32) | w[1];
+    const uint64_t v = __umul64hi(r64, p.V);
+    if (p.vidx_out) p.vidx_out[i] = v;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const uint64_t bits = (((uint64_t)w[2 + 2 * d] << 32) | w[3 + 2 * d]) >> 11;  // 53 bits
+        const double u = (double)bits * 0x1.0p-53;
+        const double orig = __dadd_rn(p.inf[d], __dmul_rn((double)p.vox[v * D + d], p.len[d]));
+        p.pos[(uint64_t)i * D + d] = __dadd_rn(orig, __dmul_rn(p.len[d], u));
+    }
+    p.key[i] = ((uint64_t)w[2 + 2 * D] << 32) | i;
+    p.rad[i] = p.radius;
+    p.cphase[i] = p.phase;
+    p.state[i] = ST_UNDECIDED;
+}
+
+// ------------------------------------------------------------------------------------------------
+// probe: a candidate overlapping a placed sphere (or its periodic image) is dead
+// (remove_collisions_with_validated_spheres, operator_cells_and_data_storage.ixx:54-76); the
+// others are linked into the candidate cell lists and appended to the alive list.
+// ------------------------------------------------------------------------------------------------
+__global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool alive = false;
+    if (i < c.n && c.state[i] == ST_UNDECIDED) {
+        double x[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
+        const double r = c.rad[i];
+        int32_t k[D];
+        cell_of<D>(g, geo, x, k);
+        const bool hit = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
+            return collide64<D>(r, x, rs, img);
+        });
+        if (hit) {
+            c.state[i] = ST_DEAD;
+        } else {
+            const int64_t idx = cell_index<D>(g, k);
+            c.cell[i] = idx;
+            c.next[i] = atomicExch(c.head + idx, (int32_t)i);
+            alive = true;
+        }
+    }
+    const uint32_t slot = warp_append(&c.counters[0], alive);
+    if (alive) c.alive[slot] = i;
+}
+
+// Visits the same-round candidates in the stencil around cell k (linked lists head/next).
+template <class F>
+__device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c,
+                                                 const int32_t* k, F&& f) {
+    for (int s = 0; s < g.S; s++) {
+        int8_t q[D];
+        const int64_t idx = stencil_cell<D>(g, k, s, q);
+        for (int32_t j = c.head[idx]; j >= 0; j = c.next[j]) {
+            double p[D], img[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) p[d] = c.pos[(uint64_t)j * D + d];
+            image_of<D>(geo, p, q, img);
+            if (f(j, img)) return;
+        }
+    }
+}
+
+__device__ __forceinline__ uint8_t load_state(const uint8_t* s, int32_t j) {
+    return *((volatile const uint8_t*)(s + j));
+}
+
+// ------------------------------------------------------------------------------------------------
+// settle: the accepted set is the sequential greedy in ascending key (find_solve_conflicts and the
+// add_to_sample loop, operator_cells_and_data_storage.ixx:79-143, operator_algorithm.ixx:383-443):
+// a candidate is accepted iff no accepted candidate of strictly smaller key overlaps it.  Computed as
+// a monotone fixpoint: collect stores each candidate's strictly-lower overlapping candidates (seen
+// from the candidate itself, i.e. against their periodic image); settle iterations then accept a
+// candidate whose blockers are all rejected and reject one with an accepted blocker.  The smallest
+// undecided key always settles, so each iteration makes progress.
+// ------------------------------------------------------------------------------------------------
+__global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    bool undecided = false;
+    if (t < nalive) {
+        const uint32_t i = c.alive[t];
+        double x[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
+        const double r = c.rad[i];
+        const uint64_t key = c.key[i];
+        int32_t k[D];
+        cell_of<D>(g, geo, x, k);
+        int nb = 0;
+        visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
+            if (!(c.key[j] < key)) return false;
+            if (!collide64<D>(r, x, c.rad[j], img)) return false;
+            if (nb < NB) c.blk[(uint64_t)i * NB + nb] = j;
+            nb++;
+            return false;
+        });
+        if (nb == 0) {
+            c.state[i] = ST_ACCEPTED;
+        } else {
+            c.nblk[i] = nb > NB ? (uint8_t)NB_OVERFLOW : (uint8_t)nb;
+            undecided = true;
+        }
+    }
+    const uint32_t mask = __ballot_sync(0xffffffffu, undecided);
+    if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[0], (uint32_t)__popc(mask));
+}
+
+__global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
+    if (c.und[it - 1] == 0) return;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    bool still = false;
+    if (t < nalive) {
+        const uint32_t i = c.alive[t];
+        if (load_state(c.state, i) == ST_UNDECIDED) {
+            bool any_acc = false, all_rej = true;
+            const uint8_t nb = c.nblk[i];
+            if (nb != NB_OVERFLOW) {
+                for (int j = 0; j < nb; j++) {
+                    const uint8_t s = load_state(c.state, c.blk[(uint64_t)i * NB + j]);
+                    any_acc |= (s == ST_ACCEPTED);
+                    all_rej &= (s == ST_REJECTED);
+                }
+            } else {
+                double x[D];
+#pragma unroll
+                for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
+                const double r = c.rad[i];
+                const uint64_t key = c.key[i];
+                int32_t k[D];
+                cell_of<D>(g, geo, x, k);
+                visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
+                    if (!(c.key[j] < key)) return false;
+                    if (!collide64<D>(r, x, c.rad[j], img)) return false;
+                    const uint8_t s = load_state(c.state, j);
+                    any_acc |= (s == ST_ACCEPTED);
+                    all_rej &= (s == ST_REJECTED);
+                    return any_acc;
+                });
+            }
+            if (any_acc) c.state[i] = ST_REJECTED;
+            else if (all_rej) c.state[i] = ST_ACCEPTED;
+            else still = true;
+        }
+    }
+    const uint32_t mask = __ballot_sync(0xffffffffu, still);
+    if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[it], (uint32_t)__popc(mask));
+}
+
+// keys of the accepted candidates, for the count cap (retain_only_first_elements)
+__global__ void k_gather_accepted(CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    bool acc = false;
+    uint32_t i = 0;
+    if (t < nalive) {
+        i = c.alive[t];
+        acc = c.state[i] == ST_ACCEPTED;
+    }
+    const uint32_t slot = warp_append(&c.counters[3], acc);
+    if (acc) c.gather[slot] = c.key[i];
+}
+
+// drops accepted candidates beyond the cap: priority (key >> 32) > pivot (reference rule) or
+// key > key_cut (exact rule)
+__global__ void k_cut_accepted(CandArgs c, int use_pivot, double pivot, uint64_t key_cut) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    if (t >= nalive) return;
+    const uint32_t i = c.alive[t];
+    if (c.state[i] != ST_ACCEPTED) return;
+    const uint64_t key = c.key[i];
+    const bool drop = use_pivot ? ((double)(key >> 32) > pivot) : (key > key_cut);
+    if (drop) c.state[i] = ST_REJECTED;
+}
+
+// commit: accepted candidates become placed spheres; the candidate lists are cleared.
+__global__ void k_commit(Grid<D> g, CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    bool acc = false;
+    if (t < nalive) {
+        const uint32_t i = c.alive[t];
+        const int64_t idx = c.cell[i];
+        c.head[idx] = -1;
+        if (c.state[i] == ST_ACCEPTED) {
+            acc = true;
+            const uint32_t bit = 1u << (idx & 31);
+            const uint32_t old = atomicOr(g.occ + (idx >> 5), bit);
+            if (old & bit) atomicOr(&c.counters[2], (uint32_t)ERR_DOUBLE_OCCUPANCY);
+#pragma unroll
+            for (int d = 0; d < D; d++) g.pos[idx * D + d] = c.pos[(uint64_t)i * D + d];
+            g.rad[idx] = c.rad[i];
+            g.phase[idx] = c.phase[i];
+        }
+    }
+    const uint32_t mask = __ballot_sync(0xffffffffu, acc);
+    if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.counters[1], (uint32_t)__popc(mask));
+}
+
+// ------------------------------------------------------------------------------------------------
+// refinement: remove_covered + subdivide_uncovered (list_of_voxels.ixx:30-100).  A parent is
+// dropped when one sphere's exclusion ball (r_s + r_min) holds all its corners; otherwise each child
+// is kept unless a sphere of the parent's prefilter list (dist^2(parent centre) < (r_s + r_min)^2,
+// get_list_of_spheres :283-307) holds all the child's corners.  Output order: parents in list order,
+// children in corner-table order (stable compaction).
+// ------------------------------------------------------------------------------------------------
+struct RefineParams {
+    uint64_t V;
+    const int32_t* vin;
+    int32_t* vout;
+    double len[D];
+    double nlen[D];
+    double inf[D];
+    double rmin;
+    uint32_t* masks;
+    uint32_t* block_counts;
+    const uint64_t* block_offsets;
+    uint32_t* err;
+};
+
+__global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> geo, RefineParams p) {
+    const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
+    uint32_t mask[MASK_WORDS];
+#pragma unroll
+    for (int w = 0; w < MASK_WORDS; w++) mask[w] = 0;
+    if (v < p.V) {
+        int32_t cc[D];
+        double orig[D], centre[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            cc[d] = p.vin[v * D + d];
+            orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cc[d], p.len[d]));
+            // center(i) = origin + (coord + 0.5) * len (list_of_voxels.ixx:154-160)
+            centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cc[d], 0.5), p.len[d]));
+        }
+        int32_t k[D];
+        cell_of<D>(g, geo, centre, k);
+        double pre[K_PRE][D];
+        double preR2[K_PRE];
+        int npre = 0;
+        bool overflow = false;
+        const bool covered = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
+            const double R = __dadd_rn(rs, p.rmin);
+            const double R2 = __dmul_rn(R, R);
+            if (!(maxcorner_dist2<D>(img, orig, p.len) > R2)) return true;  // parent fully covered
+            if (dist2_64<D>(img, centre) < R2) {
+                if (npre < K_PRE) {
+#pragma unroll
+                    for (int d = 0; d < D; d++) pre[npre][d] = img[d];
+                    preR2[npre] = R2;
+                    npre++;
+                } else {
+                    overflow = true;
+                }
+            }
+            return false;
+        });
+        if (!covered) {
+            if (overflow) atomicOr(p.err, (uint32_t)ERR_PREFILTER_OVERFLOW);
+            for (int t = 0; t < CHILDREN; t++) {
+                double corig[D];
+#pragma unroll
+                for (int d = 0; d < D; d++)
+                    corig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)(2 * cc[d] + corner_bit(t, d)), p.nlen[d]));
+                bool ccov = false;
+                for (int s = 0; s < npre && !ccov; s++) ccov = !(maxcorner_dist2<D>(pre[s], corig, p.nlen) > preR2[s]);
+                if (!ccov && overflow) {
+                    ccov = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
+                        const double R = __dadd_rn(rs, p.rmin);
+                        const double R2 = __dmul_rn(R, R);
+                        if (!(dist2_64<D>(img, centre) < R2)) return false;
+                        return !(maxcorner_dist2<D>(img, corig, p.nlen) > R2);
+                    });
+                }
+                if (!ccov) mask[t >> 5] |= 1u << (t & 31);
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < MASK_WORDS; w++) p.masks[v * MASK_WORDS + w] = mask[w];
+    }
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int w = 0; w < MASK_WORDS; w++) cnt += __popc(mask[w]);
+    uint32_t total;
+    block_exclusive_scan<REFINE_BLOCK>(cnt, &total);
+    if (threadIdx.x == 0) p.block_counts[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
+    const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
+    uint32_t mask[MASK_WORDS];
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int w = 0; w < MASK_WORDS; w++) {
+        mask[w] = v < p.V ? p.masks[v * MASK_WORDS + w] : 0u;
+        cnt += __popc(mask[w]);
+    }
+    const uint32_t local = block_exclusive_scan<REFINE_BLOCK>(cnt, nullptr);
+    if (v >= p.V || cnt == 0) return;
+    uint64_t o = p.block_offsets[blockIdx.x] + local;
+    int32_t cc[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) cc[d] = p.vin[v * D + d];
+    for (int t = 0; t < CHILDREN; t++) {
+        if (!((mask[t >> 5] >> (t & 31)) & 1u)) continue;
+#pragma unroll
+        for (int d = 0; d < D; d++) p.vout[o * D + d] = 2 * cc[d] + corner_bit(t, d);
+        o++;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// validators (operator_check_cell.ixx:8-78, rsa_data_storage.ixx:216-243) and reductions
+// ------------------------------------------------------------------------------------------------
+__global__ void k_check(Grid<D> g, Geo<D> geo, unsigned long long* overlaps, unsigned long long* misplaced) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.ncells || !occupied(g.occ, idx)) return;
+    double x[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) x[d] = g.pos[idx * D + d];
+    const double r = g.rad[idx];
+    int32_t k[D];
+    cell_of<D>(g, geo, x, k);
+    if (cell_index<D>(g, k) != idx) atomicAdd(misplaced, 1ull);
+    // stencil around the cell the sphere is stored in
+    int32_t kc[D];
+    int64_t rem = idx;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        kc[d] = (int32_t)(rem % g.n[d]);
+        rem /= g.n[d];
+    }
+    unsigned long long cnt = 0;
+    visit_placed<D>(g, geo, kc, [&](int64_t j, const double* img, double rs) {
+        if (j > idx && collide64<D>(r, x, rs, img)) cnt++;
+        return false;
+    });
+    if (cnt) atomicAdd(overlaps, cnt);
+}
+
+__global__ void k_volume_partials(Grid<D> g, double unit, double* partials) {
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < g.ncells;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        if (!occupied(g.occ, idx)) continue;
+        const double r = g.rad[idx];
+        // volumeSphere = mult * puissance<D>(R) (auxiliary/Geometry/Sphere.ixx:46-57)
+        double pw;
+        if (D == 2) pw = __dmul_rn(r, r);
+        else if (D == 3) pw = __dmul_rn(r, __dmul_rn(r, r));
+        else if (D == 4) { const double s = __dmul_rn(r, r); pw = __dmul_rn(s, s); }
+        else if (D == 5) { const double s = __dmul_rn(r, r); pw = __dmul_rn(s, __dmul_rn(r, s)); }
+        else if (D == 6) { const double s = __dmul_rn(r, __dmul_rn(r, r)); pw = __dmul_rn(s, s); }
+        else { const double s = __dmul_rn(r, __dmul_rn(r, r)); const double t = __dmul_rn(__dmul_rn(r, r), __dmul_rn(r, r)); pw = __dmul_rn(s, t); }
+        acc += __dmul_rn(unit, pw);
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(OCC_BLOCK) k_extract_write(Grid<D> g, const uint64_t* block_offsets, double* pos,
+                                                           double* rad, int32_t* phase) {
+    const int64_t nwords = (g.ncells + 31) / 32;
+    const int64_t w = (int64_t)blockIdx.x * OCC_BLOCK + threadIdx.x;
+    const uint32_t bits = w < nwords ? g.occ[w] : 0u;
+    const uint32_t local = block_exclusive_scan<OCC_BLOCK>((uint32_t)__popc(bits), nullptr);
+    uint64_t o = block_offsets[blockIdx.x] + local;
+    uint32_t b = bits;
+    while (b) {
+        const int j = __ffs(b) - 1;
+        b &= b - 1;
+        const int64_t idx = w * 32 + j;
+        if (pos) {
+#pragma unroll
+            for (int d = 0; d < D; d++) pos[o * D + d] = g.pos[idx * D + d];
+        }
+        if (rad) rad[o] = g.rad[idx];
+        if (phase) phase[o] = g.phase[idx];
+        o++;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// host launchers
+// ------------------------------------------------------------------------------------------------
+void op_vox_init(int32_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s) {
+    NVox nv;
+    for (int d = 0; d < D; d++) nv.n[d] = nvox[d];
+    if (V == 0) return;
+    k_vox_init<<<nblocks(V, 256), 256, 0, s>>>(vox, V, nv);
+    count_launch();
+}
+
+void op_darts(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaStream_t s) {
+    DartParams p;
+    p.n = a.n;
+    p.V = a.V;
+    p.vox = a.vox;
+    for (int d = 0; d < D; d++) {
+        p.len[d] = a.len[d];
+        p.inf[d] = ga.inf[d];
+    }
+    p.seed_lo = (uint32_t)a.seed;
+    p.seed_hi = (uint32_t)(a.seed >> 32);
+    p.round_lo = (uint32_t)a.round;
+    p.round_hi = (uint32_t)(a.round >> 32);
+    p.radius = a.radius;
+    p.phase = a.phase;
+    p.pos = c.pos;
+    p.key = c.key;
+    p.rad = c.rad;
+    p.cphase = c.phase;
+    p.state = c.state;
+    p.vidx_out = a.vidx_out;
+    if (a.n == 0) return;
+    k_darts<<<nblocks(a.n, 256), 256, 0, s>>>(p);
+    count_launch();
+}
+
+void op_probe(const GridArgs& ga, const CandArgs& c, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_probe<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    count_launch();
+}
+
+void op_collect(const GridArgs& ga, const CandArgs& c, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_collect<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    count_launch();
+}
+
+void op_settle(const GridArgs& ga, const CandArgs& c, int it, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_settle<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c, it);
+    count_launch();
+}
+
+void op_gather_accepted(const CandArgs& c, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_gather_accepted<<<nblocks(c.n, 256), 256, 0, s>>>(c);
+    count_launch();
+}
+
+void op_cut_accepted(const CandArgs& c, int use_pivot, double pivot, uint64_t key_cut, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_cut_accepted<<<nblocks(c.n, 256), 256, 0, s>>>(c, use_pivot, pivot, key_cut);
+    count_launch();
+}
+
+void op_commit(const GridArgs& ga, const CandArgs& c, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_commit<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), c);
+    count_launch();
+}
+
+RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
+    RefineParams p;
+    p.V = a.V;
+    p.vin = a.vin;
+    p.vout = a.vout;
+    for (int d = 0; d < D; d++) {
+        p.len[d] = a.len[d];
+        p.nlen[d] = a.nlen[d];
+        p.inf[d] = ga.inf[d];
+    }
+    p.rmin = a.rmin;
+    p.masks = a.masks;
+    p.block_counts = a.block_counts;
+    p.block_offsets = a.block_offsets;
+    p.err = a.err;
+    return p;
+}
+
+void op_refine_mask(const GridArgs& ga, const RefineArgs& a, cudaStream_t s) {
+    if (a.V == 0) return;
+    k_refine_mask<<<nblocks(a.V, REFINE_BLOCK), REFINE_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
+    count_launch();
+}
+
+void op_refine_write(const RefineArgs& a, cudaStream_t s) {
+    if (a.V == 0) return;
+    GridArgs none{};  // the write pass needs no geometry
+    k_refine_write<<<nblocks(a.V, REFINE_BLOCK), REFINE_BLOCK, 0, s>>>(make_refine(none, a));
+    count_launch();
+}
+
+void op_check(const GridArgs& ga, unsigned long long* overlaps, unsigned long long* misplaced, cudaStream_t s) {
+    k_check<<<nblocks(ga.ncells, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), overlaps, misplaced);
+    count_launch();
+}
+
+void op_volume_partials(const GridArgs& ga, double unit, double* partials, int nb, cudaStream_t s) {
+    k_volume_partials<<<nb, 256, 0, s>>>(make_grid(ga), unit, partials);
+    count_launch();
+}
+
+void op_extract_write(const GridArgs& ga, const uint64_t* block_offsets, double* pos, double* rad, int32_t* phase,
+                      cudaStream_t s) {
+    const int64_t nwords = (ga.ncells + 31) / 32;
+    k_extract_write<<<nblocks(nwords, OCC_BLOCK), OCC_BLOCK, 0, s>>>(make_grid(ga), block_offsets, pos, rad, phase);
+    count_launch();
+}
+
+const DimOps kOps = {
+    D,
+    op_vox_init,
+    op_darts,
+    op_probe,
+    op_collect,
+    op_settle,
+    op_gather_accepted,
+    op_cut_accepted,
+    op_commit,
+    op_refine_mask,
+    op_refine_write,
+    op_check,
+    op_volume_partials,
+    op_extract_write,
+    CHILDREN,
+    MASK_WORDS,
+};
+
+}  // namespace
+
+#define RSA_CAT2(a, b) a##b
+#define RSA_CAT(a, b) RSA_CAT2(a, b)
+const DimOps* RSA_CAT(dim_ops_, RSA_DIM)() { return &kOps; }
+
+}  // namespace rsagpu

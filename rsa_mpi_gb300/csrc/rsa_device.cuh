@@ -1,0 +1,217 @@
+// rsa_device.cuh -- device code of the GB300 sampler, templated on the space dimension D.
+//
+// Data layout in HBM (one sampler instance):
+//   sphere grid  : cells of edge c_d = L_d / n_d with c * sqrt(D) < 2 r_min, so that a cell holds at
+//                  most one accepted centre.  occ = 1 bit per cell (10 MB for 434^3 cells, L2
+//                  resident); pos = D doubles per cell, rad = 1 double per cell, phase = int32 per
+//                  cell (all indexed by the cell, so the cell index IS the sphere id).
+//   voxel list   : AoS int32[V][D] integer coordinates at the current level, one length per level.
+//   candidates   : SoA per round (pos, key, rad, phase, cell, state, next) + a per-cell list head.
+//
+// Every FP64 decision uses __dadd_rn / __dsub_rn / __dmul_rn in the operation order of the
+// reference line it restates, so nothing is contracted into an FMA and every comparison rounds as
+// the reference's does (is_there_collision operator_cells_and_data_storage.ixx:5-14,
+// is_in_sphere list_of_voxels.ixx:225-238, get_list_of_spheres :283-307, pick_points :107-129).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rsagpu {
+
+enum : uint8_t { ST_DEAD = 0, ST_UNDECIDED = 1, ST_ACCEPTED = 2, ST_REJECTED = 3 };
+
+// error bits written by kernels
+enum : uint32_t {
+    ERR_DOUBLE_OCCUPANCY = 1u,   // two accepted centres in one cell
+    ERR_BLOCKER_OVERFLOW = 2u,   // (informational) a candidate had more than NB lower colliders
+    ERR_PREFILTER_OVERFLOW = 4u, // (informational) a parent voxel had more than K prefilter spheres
+};
+
+constexpr int NB = 8;      // stored lower-priority colliders per candidate
+constexpr int NB_OVERFLOW = 255;
+
+template <int D>
+struct Geo {
+    double inf[D];
+    double L[D];
+};
+
+template <int D>
+struct Grid {
+    int64_t ncells;
+    int32_t n[D];
+    double inv_c[D];
+    uint32_t* occ;
+    double* pos;
+    double* rad;
+    int32_t* phase;
+    const int8_t* stencil;  // S offsets of D int8
+    int S;
+};
+
+// ---------------------------------------------------------------------------------------------
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy as 1, 2, 3", SC'11)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t lo0 = c.x * 0xD2511F53u, hi0 = __umulhi(c.x, 0xD2511F53u);
+        const uint32_t lo1 = c.z * 0xCD9E8D57u, hi1 = __umulhi(c.z, 0xCD9E8D57u);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// ---------------------------------------------------------------------------------------------
+// geometry, exact FP64
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ bool collide64(double r1, const double* a, double r2, const double* b) {
+    double dist2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const double dr = __dsub_rn(a[d], b[d]);
+        dist2 = __dadd_rn(dist2, __dmul_rn(dr, dr));
+    }
+    const double rr = __dadd_rn(r1, r2);
+    return dist2 < __dmul_rn(rr, rr);
+}
+
+// max over the 2^D corners {orig + t * len, t in {0,1}^D} of the reference's rounded corner distance
+// sum_d (corner_d - delta_d)^2 with delta = img - orig.  Round-to-nearest addition is monotone in each
+// operand, so the largest rounded sum is the rounded sum of the per-dimension largest terms: one
+// evaluation equals the reference's 2^D-corner loop bit for bit.
+template <int D>
+__device__ __forceinline__ double maxcorner_dist2(const double* img, const double* orig, const double* len) {
+    double dist2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const double delta = __dsub_rn(img[d], orig[d]);
+        const double t0 = __dsub_rn(0.0, delta);
+        const double t1 = __dsub_rn(len[d], delta);
+        const double s0 = __dmul_rn(t0, t0), s1 = __dmul_rn(t1, t1);
+        dist2 = __dadd_rn(dist2, s0 > s1 ? s0 : s1);
+    }
+    return dist2;
+}
+
+template <int D>
+__device__ __forceinline__ double dist2_64(const double* a, const double* b) {
+    double dist2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const double t = __dsub_rn(a[d], b[d]);
+        dist2 = __dadd_rn(dist2, __dmul_rn(t, t));
+    }
+    return dist2;
+}
+
+template <int D>
+__device__ __forceinline__ void cell_of(const Grid<D>& g, const Geo<D>& geo, const double* x, int32_t* k) {
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        int32_t kk = (int32_t)floor(__dmul_rn(__dsub_rn(x[d], geo.inf[d]), g.inv_c[d]));
+        kk = kk < 0 ? 0 : (kk >= g.n[d] ? g.n[d] - 1 : kk);
+        k[d] = kk;
+    }
+}
+
+template <int D>
+__device__ __forceinline__ int64_t cell_index(const Grid<D>& g, const int32_t* k) {
+    int64_t idx = 0;
+#pragma unroll
+    for (int d = D - 1; d >= 0; d--) idx = idx * g.n[d] + k[d];
+    return idx;
+}
+
+// Wrapped stencil cell s around cell k: linear index and per-dimension image shift q in {-1,0,1}.
+template <int D>
+__device__ __forceinline__ int64_t stencil_cell(const Grid<D>& g, const int32_t* k, int s, int8_t* q) {
+    int64_t idx = 0;
+#pragma unroll
+    for (int d = D - 1; d >= 0; d--) {
+        int32_t kk = k[d] + (int32_t)g.stencil[s * D + d];
+        int8_t qq = 0;
+        if (kk < 0) { kk += g.n[d]; qq = -1; }
+        else if (kk >= g.n[d]) { kk -= g.n[d]; qq = 1; }
+        q[d] = qq;
+        idx = idx * g.n[d] + kk;
+    }
+    return idx;
+}
+
+// image of a stored centre: x + q L per wrapped dimension (the reference's ghost copy x + (+-L),
+// rsa_ghost_area.ixx:22-30)
+template <int D>
+__device__ __forceinline__ void image_of(const Geo<D>& geo, const double* p, const int8_t* q, double* img) {
+#pragma unroll
+    for (int d = 0; d < D; d++) img[d] = q[d] == 0 ? p[d] : __dadd_rn(p[d], q[d] > 0 ? geo.L[d] : -geo.L[d]);
+}
+
+__device__ __forceinline__ bool occupied(const uint32_t* occ, int64_t idx) {
+    return (__ldg(occ + (idx >> 5)) >> (idx & 31)) & 1u;
+}
+
+// Visits the placed spheres in the stencil around cell k; f(idx, img, r) returns true to stop.
+template <int D, class F>
+__device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo, const int32_t* k, F&& f) {
+    for (int s = 0; s < g.S; s++) {
+        int8_t q[D];
+        const int64_t idx = stencil_cell<D>(g, k, s, q);
+        if (!occupied(g.occ, idx)) continue;
+        double p[D], img[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) p[d] = g.pos[idx * D + d];
+        image_of<D>(geo, p, q, img);
+        if (f(idx, img, g.rad[idx])) return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------------------------
+// warp / block helpers
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+    const uint32_t mask = __activemask();
+    const uint32_t ballot = __ballot_sync(mask, pred);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader && ballot) base = atomicAdd(counter, (uint32_t)__popc(ballot));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(ballot & ((1u << lane) - 1u));
+}
+
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t warp_sums[BLOCK / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < BLOCK / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < BLOCK / 32) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t warp_prefix = warp > 0 ? warp_sums[warp - 1] : 0;
+    if (total) *total = warp_sums[BLOCK / 32 - 1];
+    const uint32_t r = warp_prefix + x - v;
+    __syncthreads();
+    return r;
+}
+
+}  // namespace rsagpu

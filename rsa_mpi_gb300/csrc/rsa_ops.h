@@ -1,0 +1,101 @@
+// rsa_ops.h -- host-side launch interface of the per-dimension kernel sets.
+// kernels.cu is compiled once per dimension D (-DRSA_DIM=D) and exports dim_ops_D(); the host driver
+// (rsagpu.cu) picks the table for the instance's dimension.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rsagpu {
+
+constexpr int MAX_D = 7;
+
+struct GridArgs {
+    int64_t ncells;
+    int32_t n[MAX_D];
+    double inv_c[MAX_D];
+    double inf[MAX_D];
+    double L[MAX_D];
+    uint32_t* occ;
+    double* pos;
+    double* rad;
+    int32_t* phase;
+    const int8_t* stencil;
+    int S;
+};
+
+struct CandArgs {
+    uint32_t n;         // candidates in the round
+    double* pos;        // n * D
+    uint64_t* key;      // priority key (smaller first)
+    double* rad;
+    int32_t* phase;
+    int64_t* cell;      // sphere-grid cell of the candidate
+    uint8_t* state;     // ST_*
+    int32_t* next;      // linked list of candidates per cell
+    int32_t* head;      // per grid cell, -1 = no candidate
+    uint32_t* alive;    // candidates that survived the probe
+    uint32_t* counters; // [0] = alive count, [1] = accepted count, [2] = error bits, [3] = gathered
+    int32_t* blk;       // NB lower-priority colliders per candidate
+    uint8_t* nblk;
+    uint32_t* und;      // undecided count after each settle iteration (und[0] after collect)
+    uint64_t* gather;   // keys of accepted candidates (count cap)
+};
+
+struct DartArgs {
+    uint32_t n;
+    uint64_t V;
+    const int32_t* vox;
+    double len[MAX_D];
+    uint64_t seed;
+    uint64_t round;
+    double radius;
+    int32_t phase;
+    uint64_t* vidx_out;  // optional: chosen voxel per dart
+};
+
+struct RefineArgs {
+    uint64_t V;
+    const int32_t* vin;
+    int32_t* vout;
+    double len[MAX_D];   // parent length
+    double nlen[MAX_D];  // child length = 0.5 * parent
+    double rmin;
+    uint32_t* masks;     // W words per parent
+    uint32_t* block_counts;
+    uint64_t* block_offsets;
+    uint32_t* err;
+};
+
+struct DimOps {
+    int D;
+    void (*vox_init)(int32_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s);
+    void (*darts)(const GridArgs& g, const CandArgs& c, const DartArgs& a, cudaStream_t s);
+    void (*probe)(const GridArgs& g, const CandArgs& c, cudaStream_t s);
+    void (*collect)(const GridArgs& g, const CandArgs& c, cudaStream_t s);
+    void (*settle)(const GridArgs& g, const CandArgs& c, int iteration, cudaStream_t s);
+    void (*gather_accepted)(const CandArgs& c, cudaStream_t s);
+    void (*cut_accepted)(const CandArgs& c, int use_pivot, double pivot, uint64_t key_cut, cudaStream_t s);
+    void (*commit)(const GridArgs& g, const CandArgs& c, cudaStream_t s);
+    void (*refine_mask)(const GridArgs& g, const RefineArgs& a, cudaStream_t s);
+    void (*refine_write)(const RefineArgs& a, cudaStream_t s);
+    void (*check)(const GridArgs& g, unsigned long long* overlaps, unsigned long long* misplaced, cudaStream_t s);
+    void (*volume_partials)(const GridArgs& g, double unit_volume, double* partials, int nblocks, cudaStream_t s);
+    void (*extract_write)(const GridArgs& g, const uint64_t* block_offsets, double* pos, double* rad,
+                          int32_t* phase, cudaStream_t s);
+    int children;      // 2^D
+    int mask_words;    // 32-bit words of child mask per voxel
+};
+
+const DimOps* dim_ops(int D);
+
+// dimension-independent kernels (kernels_common.cu)
+void launch_scan_blocks(const uint32_t* counts, uint64_t* offsets, uint64_t n, uint64_t* total, cudaStream_t s);
+void launch_occ_block_counts(const uint32_t* occ, int64_t nwords, uint32_t* counts, cudaStream_t s);
+uint64_t kernel_launch_count();
+void count_launch(int n = 1);
+
+constexpr int REFINE_BLOCK = 256;
+constexpr int OCC_BLOCK = 256;  // words per extract block
+
+}  // namespace rsagpu

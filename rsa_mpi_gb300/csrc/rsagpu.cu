@@ -1,0 +1,1171 @@
+// rsagpu.cu -- host driver and C ABI of the GB300 sampler (include/rsagpu.h).
+//
+// The round loop restates rsa_algo::proceed_voxel (operator_algorithm.ixx:85-188) with device-resident
+// state: the whole periodic domain lives in one device cell grid, so the reference's MPI ghost exchange
+// (operator_ghost, rsa_ghost_area, rsa_buffer) becomes periodic index wrap inside the kernels and its
+// Allreduce counters become device counters read once per round.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rsagpu.h"
+#include "rsa_device.cuh"
+#include "rsa_ops.h"
+
+using namespace rsagpu;
+
+// ------------------------------------------------------------------------------------------------
+// errors
+// ------------------------------------------------------------------------------------------------
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+struct CudaError {
+    int code;
+};
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            fail(RSAGPU_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                 __LINE__);                                                                        \
+            throw CudaError{RSAGPU_ERR_CUDA};                                                      \
+        }                                                                                          \
+    } while (0)
+
+struct Fail {
+    int code;
+};
+
+[[noreturn]] void raise(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    throw Fail{code};
+}
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return RSAGPU_OK;
+    } catch (const CudaError& e) {
+        return e.code;
+    } catch (const Fail& e) {
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        return fail(RSAGPU_ERR_CAPACITY, "host allocation failed");
+    }
+}
+
+template <class T>
+T* dalloc(uint64_t n) {
+    if (n == 0) n = 1;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        raise(RSAGPU_ERR_CUDA, "cudaMalloc of %llu bytes failed: %s", (unsigned long long)(n * sizeof(T)),
+              cudaGetErrorString(e));
+    }
+    return (T*)p;
+}
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// v_D(r) as volumeSphere (auxiliary/Geometry/Sphere.ixx:30-57): mult * puissance<D>(r)
+double pow_int(double x, int e) {
+    if (e == 0) return 1;
+    if (e == 1) return x;
+    int e1 = e / 2;
+    return pow_int(x, e1) * pow_int(x, e - e1);
+}
+double unit_ball_volume(int D) {
+    const double pi = 3.14159265358979323846;
+    double mult = 1;
+    if (D % 2 == 0) {
+        for (int k = 0; k <= D / 2 - 1; k++) mult *= (2 * pi) / (D - 2 * k);
+    } else {
+        mult = 1. / pi;
+        for (int k = 0; k <= (D - 1) / 2; k++) mult *= (2 * pi) / (D - 2 * k);
+    }
+    return mult;
+}
+double ball_volume(int D, double r) { return unit_ball_volume(D) * pow_int(r, D); }
+
+// magical_default_miss_rate (operator_algorithm.ixx:344-351)
+double reference_miss_threshold(int D) { return D <= 3 ? 0.95 : 1 - 0.05 * pow_int(0.1, D - 3); }
+
+struct TraceRow {
+    uint64_t voxels, darts, accepted;
+    uint8_t refined;
+    int32_t level;
+};
+
+constexpr int MAX_SETTLE = 4096;
+constexpr int COUNTERS = 8;
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// handles
+// ------------------------------------------------------------------------------------------------
+struct rsagpu_radgen {
+    int dim = 0;
+    std::vector<double> r;
+    std::vector<uint64_t> n;
+    std::vector<int> phase;
+    double excl = 0;
+    int idx = 0;
+    double rmax() const { return r.front(); }
+    double rmin() const { return r.back(); }
+};
+
+struct SphereGrid {
+    bool ready = false;
+    double rmin = 0, rmax = 0;
+    GridArgs a{};
+    std::vector<int8_t> stencil;
+    int8_t* d_stencil = nullptr;
+    int32_t* head = nullptr;
+    void release() {
+        dfree(a.occ);
+        dfree(a.pos);
+        dfree(a.rad);
+        dfree(a.phase);
+        dfree(d_stencil);
+        dfree(head);
+        ready = false;
+    }
+};
+
+struct rsagpu_domain {
+    int dim = 0;
+    int device = 0;
+    double inf[MAX_D]{}, sup[MAX_D]{}, L[MAX_D]{};
+    double rad_max = 0;
+    SphereGrid grid;
+    cudaStream_t stream = nullptr;
+    ~rsagpu_domain() { grid.release(); }
+};
+
+struct CandBuffers {
+    uint64_t cap = 0;
+    CandArgs a{};
+    uint64_t* vidx = nullptr;
+    void release() {
+        dfree(a.pos);
+        dfree(a.key);
+        dfree(a.rad);
+        dfree(a.phase);
+        dfree(a.cell);
+        dfree(a.state);
+        dfree(a.next);
+        dfree(a.alive);
+        dfree(a.counters);
+        dfree(a.blk);
+        dfree(a.nblk);
+        dfree(a.gather);
+        dfree(vidx);
+        cap = 0;
+    }
+};
+
+struct rsagpu_algo {
+    rsagpu_domain* dom = nullptr;
+    rsagpu_radgen rg;
+    int nbshots = 6000;
+    const DimOps* ops = nullptr;
+    cudaStream_t stream = nullptr;
+    // voxels
+    int32_t* vox[2] = {nullptr, nullptr};
+    uint64_t vox_cap[2] = {0, 0};
+    int cur = 0;
+    uint64_t V = 0;
+    int level = 0;
+    int64_t nvox0[MAX_D]{};
+    double len[MAX_D]{};
+    uint32_t* masks = nullptr;
+    uint64_t masks_cap = 0;
+    uint32_t* block_counts = nullptr;
+    uint64_t* block_offsets = nullptr;
+    uint64_t blocks_cap = 0;
+    uint32_t* d_err = nullptr;
+    // candidates
+    CandBuffers cand;
+    uint32_t* h_counters = nullptr;  // pinned mirror: COUNTERS + MAX_SETTLE + 1
+    // schedule
+    int form = RSAGPU_FORM_FP64, schedule = RSAGPU_SCHEDULE_HEURISTIC, cap_rule = RSAGPU_CAP_REFERENCE;
+    double factor = 1.0, miss_thr = -1.0;
+    uint64_t min_darts = 4096, max_darts = 1ull << 25;
+    std::vector<uint16_t> mlp;
+    // state
+    bool begun = false;
+    uint64_t seed = 0, round = 0;
+    std::vector<TraceRow> trace;
+    rsagpu_stats stats{};
+    bool timing = false;
+    cudaEvent_t ev[12]{};
+    ~rsagpu_algo() {
+        cand.release();
+        dfree(vox[0]);
+        dfree(vox[1]);
+        dfree(masks);
+        dfree(block_counts);
+        dfree(block_offsets);
+        dfree(d_err);
+        if (h_counters) cudaFreeHost(h_counters);
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+void set_device(const rsagpu_domain* d) { CK(cudaSetDevice(d->device)); }
+
+// ------------------------------------------------------------------------------------------------
+// sphere grid: cells of edge c with c sqrt(D) < 2 r_min (at most one accepted centre per cell) and
+// a stencil of every cell within 2 r_max (the largest centre distance any decision looks at).
+// ------------------------------------------------------------------------------------------------
+void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
+    const int D = dom->dim;
+    SphereGrid& G = dom->grid;
+    G.release();
+    G.rmin = rmin;
+    G.rmax = rmax;
+    GridArgs& a = G.a;
+    a = GridArgs{};
+    int64_t ncells = 1;
+    double c[MAX_D];
+    for (int d = 0; d < D; d++) {
+        int n = 1 + (int)(std::sqrt((double)D) * dom->L[d] / (2 * rmin));
+        while (dom->L[d] / n * std::sqrt((double)D) >= 2 * rmin * (1 - 1e-9)) n++;
+        a.n[d] = n;
+        c[d] = dom->L[d] / n;
+        a.inv_c[d] = 1.0 / c[d];
+        a.inf[d] = dom->inf[d];
+        a.L[d] = dom->L[d];
+        ncells *= n;
+        if (ncells > (int64_t)1 << 40) raise(RSAGPU_ERR_CAPACITY, "cell grid too large");
+    }
+    a.ncells = ncells;
+    const double R = 2 * rmax;
+    int w[MAX_D];
+    for (int d = 0; d < D; d++) {
+        w[d] = (int)std::floor(R / c[d]) + 1;
+        if (w[d] > a.n[d])
+            raise(RSAGPU_ERR_ARG, "box too small for radius %g: %d cells along dimension %d", rmax, a.n[d], d);
+        if (w[d] > 127) raise(RSAGPU_ERR_CAPACITY, "radius ratio too large for the stencil");
+    }
+    // offsets o with sum_d (max(0, |o_d| - 1) c_d)^2 <= R^2, sorted by |o|^2 (own cell first)
+    std::vector<std::vector<int8_t>> offs;
+    std::vector<int> o(D);
+    for (int d = 0; d < D; d++) o[d] = -w[d];
+    while (true) {
+        double lb = 0;
+        for (int d = 0; d < D; d++) {
+            double t = std::max(0, std::abs(o[d]) - 1) * c[d];
+            lb += t * t;
+        }
+        if (lb <= R * R * (1 + 1e-9)) {
+            std::vector<int8_t> v(D);
+            for (int d = 0; d < D; d++) v[d] = (int8_t)o[d];
+            offs.push_back(v);
+        }
+        int d = 0;
+        for (; d < D; d++) {
+            if (++o[d] <= w[d]) break;
+            o[d] = -w[d];
+        }
+        if (d == D) break;
+    }
+    std::stable_sort(offs.begin(), offs.end(), [](const std::vector<int8_t>& x, const std::vector<int8_t>& y) {
+        int nx = 0, ny = 0;
+        for (size_t d = 0; d < x.size(); d++) {
+            nx += x[d] * x[d];
+            ny += y[d] * y[d];
+        }
+        return nx < ny;
+    });
+    G.stencil.clear();
+    for (auto& v : offs) G.stencil.insert(G.stencil.end(), v.begin(), v.end());
+    a.S = (int)offs.size();
+    G.d_stencil = dalloc<int8_t>(G.stencil.size());
+    CK(cudaMemcpy(G.d_stencil, G.stencil.data(), G.stencil.size(), cudaMemcpyHostToDevice));
+    a.stencil = G.d_stencil;
+    const int64_t nwords = (ncells + 31) / 32;
+    a.occ = dalloc<uint32_t>(nwords);
+    a.pos = dalloc<double>((uint64_t)ncells * D);
+    a.rad = dalloc<double>(ncells);
+    a.phase = dalloc<int32_t>(ncells);
+    G.head = dalloc<int32_t>(ncells);
+    CK(cudaMemset(a.occ, 0, nwords * sizeof(uint32_t)));
+    CK(cudaMemset(G.head, 0xFF, ncells * sizeof(int32_t)));
+    G.ready = true;
+}
+
+void ensure_cand(rsagpu_algo* A, uint64_t n) {
+    CandBuffers& C = A->cand;
+    const int D = A->dom->dim;
+    if (!C.a.counters) {
+        C.a.counters = dalloc<uint32_t>(COUNTERS + MAX_SETTLE + 1);
+        A->h_counters = nullptr;
+        CK(cudaMallocHost(&A->h_counters, (COUNTERS + MAX_SETTLE + 1) * sizeof(uint32_t)));
+    }
+    if (n <= C.cap) return;
+    uint32_t* keep = C.a.counters;
+    C.a.counters = nullptr;
+    C.release();
+    C.a.counters = keep;
+    const uint64_t cap = std::max<uint64_t>(n, 1024);
+    if (cap > 0x7fffffffull) raise(RSAGPU_ERR_CAPACITY, "more than 2^31 candidates in one round");
+    C.a.pos = dalloc<double>(cap * D);
+    C.a.key = dalloc<uint64_t>(cap);
+    C.a.rad = dalloc<double>(cap);
+    C.a.phase = dalloc<int32_t>(cap);
+    C.a.cell = dalloc<int64_t>(cap);
+    C.a.state = dalloc<uint8_t>(cap);
+    C.a.next = dalloc<int32_t>(cap);
+    C.a.alive = dalloc<uint32_t>(cap);
+    C.a.blk = dalloc<int32_t>(cap * NB);
+    C.a.nblk = dalloc<uint8_t>(cap);
+    C.a.gather = dalloc<uint64_t>(cap);
+    C.vidx = dalloc<uint64_t>(cap);
+    C.cap = cap;
+}
+
+CandArgs cand_args(rsagpu_algo* A, uint32_t n) {
+    CandArgs c = A->cand.a;
+    c.n = n;
+    c.head = A->dom->grid.head;
+    c.und = c.counters + COUNTERS;
+    return c;
+}
+
+void ensure_vox(rsagpu_algo* A, int which, uint64_t n) {
+    const int D = A->dom->dim;
+    if (n <= A->vox_cap[which]) return;
+    uint64_t cap = std::max<uint64_t>(n, A->vox_cap[which] + A->vox_cap[which] / 2);
+    dfree(A->vox[which]);
+    A->vox[which] = dalloc<int32_t>(cap * D);
+    A->vox_cap[which] = cap;
+}
+
+void ensure_refine_buffers(rsagpu_algo* A, uint64_t V) {
+    const uint64_t words = V * A->ops->mask_words;
+    if (words > A->masks_cap) {
+        dfree(A->masks);
+        A->masks_cap = std::max<uint64_t>(words, A->masks_cap + A->masks_cap / 2);
+        A->masks = dalloc<uint32_t>(A->masks_cap);
+    }
+    const uint64_t blocks = (V + REFINE_BLOCK - 1) / REFINE_BLOCK + 1;
+    const uint64_t oblocks = ((uint64_t)((A->dom->grid.a.ncells + 31) / 32) + OCC_BLOCK - 1) / OCC_BLOCK + 1;
+    const uint64_t need = std::max(blocks, oblocks);
+    if (need > A->blocks_cap) {
+        dfree(A->block_counts);
+        dfree(A->block_offsets);
+        A->blocks_cap = std::max<uint64_t>(need, A->blocks_cap + A->blocks_cap / 2);
+        A->block_counts = dalloc<uint32_t>(A->blocks_cap);
+        A->block_offsets = dalloc<uint64_t>(A->blocks_cap + 1);
+    }
+}
+
+void begin(rsagpu_algo* A) {
+    const int D = A->dom->dim;
+    // list_of_voxels(origin, L, r_max + r_min): n_d = 1 + int(sqrt(D) L_d / diag), len_d = L_d / n_d
+    // (list_of_voxels.ixx:11-28, 192-211)
+    const double diag = A->rg.rmax() + A->rg.rmin();
+    uint64_t V = 1;
+    for (int d = 0; d < D; d++) {
+        A->nvox0[d] = 1 + (int)(std::sqrt((double)D) * A->dom->L[d] / diag);
+        A->len[d] = A->dom->L[d] / (double)A->nvox0[d];
+        V *= (uint64_t)A->nvox0[d];
+    }
+    ensure_vox(A, 0, V);
+    A->cur = 0;
+    A->V = V;
+    A->level = 0;
+    A->ops->vox_init(A->vox[0], V, A->nvox0, A->stream);
+    A->begun = true;
+    A->round = 0;
+    A->trace.clear();
+    A->stats = rsagpu_stats{};
+    A->stats.peak_voxels = V;
+}
+
+// remove_covered + subdivide_uncovered (list_of_voxels.ixx:30-100)
+void refine(rsagpu_algo* A) {
+    const int D = A->dom->dim;
+    if (A->V == 0) return;
+    for (int d = 0; d < D; d++)
+        if ((double)A->nvox0[d] * std::ldexp(1.0, A->level + 1) > 2147483647.0)
+            raise(RSAGPU_ERR_CAPACITY, "voxel coordinates overflow int32 at level %d", A->level + 1);
+    ensure_refine_buffers(A, A->V);
+    RefineArgs r{};
+    r.V = A->V;
+    r.vin = A->vox[A->cur];
+    for (int d = 0; d < D; d++) {
+        r.len[d] = A->len[d];
+        r.nlen[d] = 0.5 * A->len[d];
+    }
+    r.rmin = A->rg.rmin();
+    r.masks = A->masks;
+    r.block_counts = A->block_counts;
+    r.block_offsets = A->block_offsets;
+    r.err = A->d_err;
+    const uint64_t nb = (A->V + REFINE_BLOCK - 1) / REFINE_BLOCK;
+    A->ops->refine_mask(A->dom->grid.a, r, A->stream);
+    launch_scan_blocks(A->block_counts, A->block_offsets, nb, nullptr, A->stream);
+    uint64_t total = 0;
+    CK(cudaMemcpyAsync(&total, A->block_offsets + nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, A->stream));
+    CK(cudaStreamSynchronize(A->stream));
+    const int other = 1 - A->cur;
+    ensure_vox(A, other, total);
+    r.vout = A->vox[other];
+    A->ops->refine_write(r, A->stream);
+    A->cur = other;
+    A->V = total;
+    A->level++;
+    for (int d = 0; d < D; d++) A->len[d] = r.nlen[d];
+    A->stats.refinements++;
+    A->stats.peak_voxels = std::max(A->stats.peak_voxels, total);
+}
+
+// median_of_medians::find_pivot_for_first_elements with one rank (median_of_medians.ixx:8-157):
+// the pivot retain_only_first_elements compares priorities with.  Returns false where the reference
+// throws.
+uint64_t pivot_count(const std::vector<uint64_t>& v, double pivot) {
+    const uint64_t pv = (uint64_t)pivot;
+    return (uint64_t)(std::upper_bound(v.begin(), v.end(), pv) - v.begin());
+}
+
+bool reference_pivot(std::vector<uint64_t> v, int64_t n_first, double* out) {
+    const int64_t n = (int64_t)v.size();
+    if (n_first > n || n_first <= 0 || n == 0) return false;
+    const double pct = n_first / (1. * n);
+    std::sort(v.begin(), v.end());
+    int64_t piv = (int64_t)(n * pct) - 1;
+    int64_t mn = piv, mx = piv + 1;
+    if (std::fabs(n * pct - 1 - piv) < 1e-8) mn -= 1;
+    if (mn < 0) mn = 0;
+    if (std::fabs(n * pct - 1 - piv - 1) < 1e-8) mx += 1;
+    if (mx > n - 1) mx = n - 1;
+    double cand[2] = {(double)v[mn] - 2.220446049250313e-16, (double)v[mx] + 2.220446049250313e-16};
+    if ((uint64_t)cand[1] < (uint64_t)cand[0]) std::swap(cand[0], cand[1]);
+    int p = 2;
+    for (int i = 0; i < 2; i++)
+        if ((uint64_t)n_first <= pivot_count(v, cand[i])) {
+            p = i;
+            break;
+        }
+    if (p == 2) return false;
+    double pmax = cand[p], pivot = pmax;
+    uint64_t below = pivot_count(v, pivot);
+    if (below != (uint64_t)n_first) {
+        if (p == 0) return false;
+        const double pmin = cand[p - 1];
+        double add = 0.5 * (pmax - pmin);
+        for (int j = 0; j < 20; j++) {
+            pivot = pmin + add;
+            below = pivot_count(v, pivot);
+            if (below == (uint64_t)n_first) break;
+            if (below > (uint64_t)n_first) add = 0.5 * std::fabs(add);
+            if (below < (uint64_t)n_first) add = -0.5 * std::fabs(add);
+        }
+    }
+    *out = pivot;
+    return true;
+}
+
+void ev_record(rsagpu_algo* A, int i) {
+    if (A->timing) CK(cudaEventRecord(A->ev[i], A->stream));
+}
+float ev_ms(rsagpu_algo* A, int a, int b) {
+    float ms = 0;
+    if (A->timing) cudaEventElapsedTime(&ms, A->ev[a], A->ev[b]);
+    return ms;
+}
+
+// One round on candidates already in the buffers (state = UNDECIDED): probe, settle, cap, commit.
+// Returns the number accepted.
+uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_outreach, bool keep_state) {
+    rsagpu_domain* dom = A->dom;
+    const GridArgs& g = dom->grid.a;
+    CandArgs c = cand_args(A, n);
+    const DimOps* ops = A->ops;
+    ev_record(A, 2);
+    ops->probe(g, c, A->stream);
+    ev_record(A, 3);
+    ops->collect(g, c, A->stream);
+    int it = 1;
+    const int batch = 4;
+    while (true) {
+        for (int b = 0; b < batch; b++, it++) {
+            if (it > MAX_SETTLE) raise(RSAGPU_ERR_NO_PROGRESS, "settle did not converge in %d iterations", MAX_SETTLE);
+            ops->settle(g, c, it, A->stream);
+        }
+        CK(cudaMemcpyAsync(A->h_counters + COUNTERS + it - 1, c.und + it - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                           A->stream));
+        CK(cudaStreamSynchronize(A->stream));
+        if (A->h_counters[COUNTERS + it - 1] == 0) break;
+    }
+    // settle iterations actually needed: the first zero counter
+    CK(cudaMemcpyAsync(A->h_counters + COUNTERS, c.und, sizeof(uint32_t) * it, cudaMemcpyDeviceToHost, A->stream));
+    CK(cudaStreamSynchronize(A->stream));
+    int used = 0;
+    while (used < it && A->h_counters[COUNTERS + used] != 0) used++;
+    A->stats.settle_iterations += used;
+    ev_record(A, 4);
+    if (may_outreach) {
+        ops->gather_accepted(c, A->stream);
+        CK(cudaMemcpyAsync(A->h_counters + 3, c.counters + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
+        CK(cudaStreamSynchronize(A->stream));
+        const uint64_t nacc = A->h_counters[3];
+        if (nacc > max_new) {
+            std::vector<uint64_t> keys(nacc);
+            CK(cudaMemcpyAsync(keys.data(), c.gather, nacc * sizeof(uint64_t), cudaMemcpyDeviceToHost, A->stream));
+            CK(cudaStreamSynchronize(A->stream));
+            if (A->cap_rule == RSAGPU_CAP_EXACT) {
+                uint64_t cut = 0;
+                if (max_new > 0) {
+                    std::nth_element(keys.begin(), keys.begin() + (max_new - 1), keys.end());
+                    cut = keys[max_new - 1];
+                    ops->cut_accepted(c, 0, 0.0, cut, A->stream);
+                } else {
+                    ops->cut_accepted(c, 1, -1.0, 0, A->stream);
+                }
+            } else {
+                std::vector<uint64_t> pri(nacc);
+                for (uint64_t i = 0; i < nacc; i++) pri[i] = keys[i] >> 32;
+                double pivot = 0;
+                if (!reference_pivot(pri, (int64_t)max_new, &pivot))
+                    raise(RSAGPU_ERR_PIVOT, "count-cap pivot search failed (%llu accepted, cap %llu)",
+                          (unsigned long long)nacc, (unsigned long long)max_new);
+                ops->cut_accepted(c, 1, pivot, 0, A->stream);
+            }
+        }
+    }
+    ops->commit(g, c, A->stream);
+    ev_record(A, 5);
+    CK(cudaMemcpyAsync(A->h_counters, c.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
+    CK(cudaStreamSynchronize(A->stream));
+    if (A->h_counters[2] & ERR_DOUBLE_OCCUPANCY)
+        raise(RSAGPU_ERR_INVARIANT, "two accepted centres in one grid cell");
+    (void)keep_state;
+    if (A->timing) {
+        A->stats.ms_probe += ev_ms(A, 2, 3);
+        A->stats.ms_settle += ev_ms(A, 3, 4);
+        A->stats.ms_commit += ev_ms(A, 4, 5);
+    }
+    return A->h_counters[1];
+}
+
+void reset_counters(rsagpu_algo* A) {
+    CK(cudaMemsetAsync(A->cand.a.counters, 0, (COUNTERS + MAX_SETTLE + 1) * sizeof(uint32_t), A->stream));
+}
+
+// RadiusGenerator::update_placed (radius_generator.ixx:62-68) + the miss-rate rule (operator_algorithm.ixx:
+// 140-162, 190-206).  Returns true when no class is left.
+bool end_round(rsagpu_algo* A, uint64_t n_shots, uint64_t n_new, bool* refined, double thr) {
+    rsagpu_radgen& rg = A->rg;
+    if (rg.idx < (int)rg.n.size()) {
+        rg.n[rg.idx] = rg.n[rg.idx] - n_new;
+        if (rg.n[rg.idx] == 0) rg.idx++;
+    }
+    const bool done = rg.idx >= (int)rg.n.size();
+    const double miss = (double)(n_shots - n_new) / (0.000001 + (double)n_shots);
+    *refined = false;
+    if (miss > thr) {
+        ev_record(A, 6);
+        refine(A);
+        ev_record(A, 7);
+        if (A->timing) {
+            CK(cudaEventSynchronize(A->ev[7]));
+            A->stats.ms_refine += ev_ms(A, 6, 7);
+        }
+        *refined = true;
+    }
+    return done;
+}
+
+double threshold(const rsagpu_algo* A) {
+    return A->miss_thr > 0 ? A->miss_thr : reference_miss_threshold(A->dom->dim);
+}
+
+uint64_t darts_for(const rsagpu_algo* A) {
+    const double V = (double)A->V;
+    if (A->schedule == RSAGPU_SCHEDULE_REFERENCE) {
+        // E[shots] of compute_nb_shots_voxel (operator_algorithm.ixx:208-223)
+        const double I = 0.01 * V;
+        const double m = std::min(1.0, A->nbshots / I);
+        return std::max<uint64_t>(1, (uint64_t)std::llround(m * I));
+    }
+    double c = A->factor * V;
+    c = std::max(c, (double)A->min_darts);
+    c = std::min(c, (double)A->max_darts);
+    return (uint64_t)c;
+}
+
+void proceed(rsagpu_algo* A, uint64_t seed) {
+    rsagpu_domain* dom = A->dom;
+    const int D = dom->dim;
+    // proceed_voxel builds a fresh level-0 voxel list on every call; placed spheres are kept
+    // (operator_algorithm.ixx:89-90, 238-250)
+    begin(A);
+    A->seed = seed;
+    cudaEvent_t t0, t1;
+    CK(cudaEventCreate(&t0));
+    CK(cudaEventCreate(&t1));
+    CK(cudaEventRecord(t0, A->stream));
+    const double thr = threshold(A);
+    while (true) {
+        if (A->V == 0) {
+            A->stats.maximal = 1;
+            break;
+        }
+        if (A->rg.idx >= (int)A->rg.n.size()) break;
+        const uint64_t remaining = A->rg.n[A->rg.idx];
+        uint64_t C = darts_for(A);
+        const bool may = C >= remaining;
+        ensure_cand(A, C);
+        reset_counters(A);
+        DartArgs da{};
+        da.n = (uint32_t)C;
+        da.V = A->V;
+        da.vox = A->vox[A->cur];
+        for (int d = 0; d < D; d++) da.len[d] = A->len[d];
+        da.seed = seed;
+        da.round = A->round++;
+        da.radius = A->rg.r[A->rg.idx];
+        da.phase = A->rg.phase[A->rg.idx];
+        ev_record(A, 0);
+        CandArgs c = cand_args(A, (uint32_t)C);
+        A->ops->darts(dom->grid.a, c, da, A->stream);
+        ev_record(A, 1);
+        const uint64_t n_new = decide_round(A, (uint32_t)C, remaining, may, false);
+        if (A->timing) A->stats.ms_darts += ev_ms(A, 0, 1);
+        TraceRow row{A->V, C, n_new, 0, A->level};
+        bool refined = false;
+        const bool done = end_round(A, C, n_new, &refined, thr);
+        row.refined = refined;
+        A->trace.push_back(row);
+        A->stats.rounds++;
+        A->stats.darts += C;
+        A->stats.accepted += n_new;
+        if (done) break;
+    }
+    CK(cudaEventRecord(t1, A->stream));
+    CK(cudaEventSynchronize(t1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t0, t1);
+    A->stats.ms_total += ms;
+    A->stats.final_level = A->level;
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+}
+
+uint64_t count_spheres(rsagpu_domain* dom, rsagpu_algo* helper_none) {
+    (void)helper_none;
+    const GridArgs& g = dom->grid.a;
+    if (!dom->grid.ready) return 0;
+    const int64_t nwords = (g.ncells + 31) / 32;
+    const uint64_t nb = (nwords + OCC_BLOCK - 1) / OCC_BLOCK;
+    uint32_t* counts = dalloc<uint32_t>(nb);
+    uint64_t* offs = dalloc<uint64_t>(nb + 1);
+    launch_occ_block_counts(g.occ, nwords, counts, dom->stream);
+    launch_scan_blocks(counts, offs, nb, nullptr, dom->stream);
+    uint64_t total = 0;
+    CK(cudaMemcpyAsync(&total, offs + nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, dom->stream));
+    CK(cudaStreamSynchronize(dom->stream));
+    dfree(counts);
+    dfree(offs);
+    return total;
+}
+
+rsagpu_radgen* make_radgen(int dim, const double* r, const uint64_t* n, const int* ph, int k, double excl) {
+    if (dim < 2 || dim > MAX_D) raise(RSAGPU_ERR_ARG, "dimension %d not supported (2..%d)", dim, MAX_D);
+    if (k <= 0) raise(RSAGPU_ERR_ARG, "Empty radius generator!");
+    auto* rg = new rsagpu_radgen();
+    rg->dim = dim;
+    std::vector<int> order(k);
+    for (int i = 0; i < k; i++) order[i] = i;
+    // descending radius (radius_generator.ixx:17-20)
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r[a] > r[b]; });
+    for (int i : order) {
+        if (!(r[i] > 0)) {
+            delete rg;
+            raise(RSAGPU_ERR_ARG, "radius must be positive");
+        }
+        rg->r.push_back(r[i]);
+        rg->n.push_back(n[i]);
+        rg->phase.push_back(ph ? ph[i] : 0);
+    }
+    // exclusion distance added to entry 0 once per class (radius_generator.ixx:23-25)
+    for (int i = 0; i < k; i++) rg->r[0] += 0.5 * excl;
+    rg->excl = excl;
+    return rg;
+}
+
+}  // namespace
+
+// ================================================================================================
+// C ABI
+// ================================================================================================
+extern "C" {
+
+const char* rsagpu_last_error(void) { return g_err.c_str(); }
+const char* rsagpu_version(void) { return "rsagpu 0.1 (sm_103a)"; }
+uint64_t rsagpu_kernel_launches(void) { return kernel_launch_count(); }
+
+int rsagpu_domain_create(int dim, const double* inf, const double* sup, double rad_max, rsagpu_domain** out) {
+    return guarded([&] {
+        if (!out || !inf || !sup) raise(RSAGPU_ERR_ARG, "null argument");
+        if (dim < 2 || dim > MAX_D) raise(RSAGPU_ERR_ARG, "dimension %d not supported (2..%d)", dim, MAX_D);
+        if (!(rad_max > 0)) raise(RSAGPU_ERR_ARG, "rad_max must be positive");
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            raise(RSAGPU_ERR_CUDA, "no CUDA device");
+        }
+        auto* d = new rsagpu_domain();
+        d->dim = dim;
+        cudaGetDevice(&d->device);
+        for (int i = 0; i < dim; i++) {
+            d->inf[i] = inf[i];
+            d->sup[i] = sup[i];
+            d->L[i] = sup[i] - inf[i];
+            // rsa_grid_traversal::define / check_sufficiently_large (rsa_grid_traversal.ixx:20-23,
+            // rsa_domain.ixx:135-143)
+            if (!(d->L[i] >= 2 * rad_max)) {
+                delete d;
+                raise(RSAGPU_ERR_ARG, "Too small domain wrt ghost layer");
+            }
+        }
+        d->rad_max = rad_max;
+        CK(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+        *out = d;
+    });
+}
+
+int rsagpu_domain_destroy(rsagpu_domain* dom) {
+    return guarded([&] {
+        if (!dom) return;
+        set_device(dom);
+        if (dom->stream) cudaStreamDestroy(dom->stream);
+        delete dom;
+    });
+}
+
+int rsagpu_domain_total_volume(const rsagpu_domain* dom, double* out) {
+    return guarded([&] {
+        if (!dom || !out) raise(RSAGPU_ERR_ARG, "null argument");
+        double v = 1;
+        for (int d = 0; d < dom->dim; d++) v *= dom->L[d];
+        *out = v;
+    });
+}
+
+int rsagpu_domain_count(rsagpu_domain* dom, uint64_t* out) {
+    return guarded([&] {
+        if (!dom || !out) raise(RSAGPU_ERR_ARG, "null argument");
+        set_device(dom);
+        *out = count_spheres(dom, nullptr);
+    });
+}
+
+int rsagpu_domain_spheres_volume(rsagpu_domain* dom, double* out) {
+    return guarded([&] {
+        if (!dom || !out) raise(RSAGPU_ERR_ARG, "null argument");
+        set_device(dom);
+        *out = 0;
+        if (!dom->grid.ready) return;
+        const int nb = 1024;
+        double* partials = dalloc<double>(nb);
+        dim_ops(dom->dim)->volume_partials(dom->grid.a, unit_ball_volume(dom->dim), partials, nb, dom->stream);
+        std::vector<double> h(nb);
+        CK(cudaMemcpyAsync(h.data(), partials, nb * sizeof(double), cudaMemcpyDeviceToHost, dom->stream));
+        CK(cudaStreamSynchronize(dom->stream));
+        dfree(partials);
+        double s = 0;
+        for (double x : h) s += x;
+        *out = s;
+    });
+}
+
+int rsagpu_domain_extract(rsagpu_domain* dom, double* centers, double* radii, int* phases, uint64_t cap,
+                          uint64_t* n_out) {
+    return guarded([&] {
+        if (!dom || !n_out) raise(RSAGPU_ERR_ARG, "null argument");
+        set_device(dom);
+        *n_out = 0;
+        if (!dom->grid.ready) return;
+        const GridArgs& g = dom->grid.a;
+        const int D = dom->dim;
+        const int64_t nwords = (g.ncells + 31) / 32;
+        const uint64_t nb = (nwords + OCC_BLOCK - 1) / OCC_BLOCK;
+        uint32_t* counts = dalloc<uint32_t>(nb);
+        uint64_t* offs = dalloc<uint64_t>(nb + 1);
+        launch_occ_block_counts(g.occ, nwords, counts, dom->stream);
+        launch_scan_blocks(counts, offs, nb, nullptr, dom->stream);
+        uint64_t total = 0;
+        CK(cudaMemcpyAsync(&total, offs + nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, dom->stream));
+        CK(cudaStreamSynchronize(dom->stream));
+        *n_out = total;
+        if (cap < total || (!centers && !radii && !phases)) {
+            dfree(counts);
+            dfree(offs);
+            return;
+        }
+        double* dp = centers ? dalloc<double>(total * D) : nullptr;
+        double* dr = radii ? dalloc<double>(total) : nullptr;
+        int32_t* dph = phases ? dalloc<int32_t>(total) : nullptr;
+        dim_ops(D)->extract_write(g, offs, dp, dr, dph, dom->stream);
+        if (centers) CK(cudaMemcpyAsync(centers, dp, total * D * sizeof(double), cudaMemcpyDeviceToHost, dom->stream));
+        if (radii) CK(cudaMemcpyAsync(radii, dr, total * sizeof(double), cudaMemcpyDeviceToHost, dom->stream));
+        if (phases) CK(cudaMemcpyAsync(phases, dph, total * sizeof(int32_t), cudaMemcpyDeviceToHost, dom->stream));
+        CK(cudaStreamSynchronize(dom->stream));
+        dfree(dp);
+        dfree(dr);
+        dfree(dph);
+        dfree(counts);
+        dfree(offs);
+    });
+}
+
+int rsagpu_domain_check(rsagpu_domain* dom, uint64_t* overlapping_pairs, uint64_t* misplaced) {
+    return guarded([&] {
+        if (!dom) raise(RSAGPU_ERR_ARG, "null argument");
+        set_device(dom);
+        uint64_t h[2] = {0, 0};
+        if (dom->grid.ready) {
+            unsigned long long* d = dalloc<unsigned long long>(2);
+            CK(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), dom->stream));
+            dim_ops(dom->dim)->check(dom->grid.a, d, d + 1, dom->stream);
+            CK(cudaMemcpyAsync(h, d, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, dom->stream));
+            CK(cudaStreamSynchronize(dom->stream));
+            dfree(d);
+        }
+        if (overlapping_pairs) *overlapping_pairs = h[0];
+        if (misplaced) *misplaced = h[1];
+    });
+}
+
+int rsagpu_radgen_create_counts(int dim, const double* radii, const uint64_t* counts, const int* phases,
+                                int n_classes, double exclusion_distance, rsagpu_radgen** out) {
+    return guarded([&] {
+        if (!out || !radii || !counts) raise(RSAGPU_ERR_ARG, "null argument");
+        *out = make_radgen(dim, radii, counts, phases, n_classes, exclusion_distance);
+    });
+}
+
+int rsagpu_radgen_create_fractions(int dim, const double* radii, const double* fractions, const int* phases,
+                                   int n_classes, double volume, double exclusion_distance, rsagpu_radgen** out) {
+    return guarded([&] {
+        if (!out || !radii || !fractions) raise(RSAGPU_ERR_ARG, "null argument");
+        if (n_classes <= 0) raise(RSAGPU_ERR_ARG, "Empty radius generator!");
+        std::vector<uint64_t> n(n_classes);
+        // compute_desired_radius_nb_phase (radius_generator.ixx:71-86)
+        for (int i = 0; i < n_classes; i++) n[i] = (uint64_t)(volume * fractions[i] / ball_volume(dim, radii[i]));
+        *out = make_radgen(dim, radii, n.data(), phases, n_classes, exclusion_distance);
+    });
+}
+
+int rsagpu_radgen_destroy(rsagpu_radgen* rg) {
+    delete rg;
+    return RSAGPU_OK;
+}
+
+int rsagpu_radgen_max_radius(const rsagpu_radgen* rg, double* out) {
+    if (!rg || !out) return fail(RSAGPU_ERR_ARG, "null argument");
+    *out = rg->rmax();
+    return RSAGPU_OK;
+}
+
+int rsagpu_radgen_min_radius(const rsagpu_radgen* rg, double* out) {
+    if (!rg || !out) return fail(RSAGPU_ERR_ARG, "null argument");
+    *out = rg->rmin();
+    return RSAGPU_OK;
+}
+
+int rsagpu_algo_create(rsagpu_domain* dom, const rsagpu_radgen* rg, int nbshots, rsagpu_algo** out) {
+    return guarded([&] {
+        if (!dom || !rg || !out) raise(RSAGPU_ERR_ARG, "null argument");
+        if (rg->dim != dom->dim) raise(RSAGPU_ERR_ARG, "radius generator and domain dimensions differ");
+        // operator_algorithm.ixx:27-29
+        if (rg->rmax() > dom->rad_max)
+            raise(RSAGPU_ERR_ARG,
+                  "Impossible to have the maximal radius of radius generator larger than domain implicit radius");
+        set_device(dom);
+        auto* A = new rsagpu_algo();
+        try {
+            A->dom = dom;
+            A->rg = *rg;
+            A->rg.idx = 0;
+            A->nbshots = nbshots;
+            A->ops = dim_ops(dom->dim);
+            if (!A->ops) raise(RSAGPU_ERR_ARG, "dimension not built");
+            CK(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking));
+            for (auto& e : A->ev) CK(cudaEventCreate(&e));
+            A->d_err = dalloc<uint32_t>(1);
+            CK(cudaMemset(A->d_err, 0, sizeof(uint32_t)));
+            // the algo rebuilds the domain's grid and drops its spheres (operator_algorithm.ixx:25-26)
+            build_grid(dom, rg->rmin(), std::max(rg->rmax(), 0.0));
+            ensure_cand(A, 1024);
+        } catch (...) {
+            delete A;
+            throw;
+        }
+        *out = A;
+    });
+}
+
+int rsagpu_algo_destroy(rsagpu_algo* algo) {
+    return guarded([&] {
+        if (!algo) return;
+        set_device(algo->dom);
+        delete algo;
+    });
+}
+
+int rsagpu_algo_set_form(rsagpu_algo* algo, int form, int schedule) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        if (form != RSAGPU_FORM_FP64 && form != RSAGPU_FORM_FP32_GUARD) raise(RSAGPU_ERR_ARG, "unknown form %d", form);
+        if (schedule < 0 || schedule > RSAGPU_SCHEDULE_REFERENCE) raise(RSAGPU_ERR_ARG, "unknown schedule %d", schedule);
+        algo->form = form;
+        algo->schedule = schedule;
+    });
+}
+
+int rsagpu_algo_set_cap_rule(rsagpu_algo* algo, int rule) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        if (rule != RSAGPU_CAP_REFERENCE && rule != RSAGPU_CAP_EXACT) raise(RSAGPU_ERR_ARG, "unknown cap rule");
+        algo->cap_rule = rule;
+    });
+}
+
+int rsagpu_algo_set_schedule_params(rsagpu_algo* algo, double factor, uint64_t min_darts, uint64_t max_darts,
+                                    double miss_threshold) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        if (!(factor > 0) || min_darts == 0 || max_darts < min_darts || max_darts > 0x7fffffffull)
+            raise(RSAGPU_ERR_ARG, "invalid schedule parameters");
+        algo->factor = factor;
+        algo->min_darts = min_darts;
+        algo->max_darts = max_darts;
+        algo->miss_thr = miss_threshold;
+    });
+}
+
+int rsagpu_algo_set_mlp(rsagpu_algo* algo, const uint16_t* w, uint64_t n) {
+    return guarded([&] {
+        if (!algo || !w) raise(RSAGPU_ERR_ARG, "null argument");
+        if (n != 5378) raise(RSAGPU_ERR_ARG, "expected 5378 weights, got %llu", (unsigned long long)n);
+        algo->mlp.assign(w, w + n);
+    });
+}
+
+int rsagpu_algo_set_timing(rsagpu_algo* algo, int on) {
+    if (!algo) return fail(RSAGPU_ERR_ARG, "null argument");
+    algo->timing = on != 0;
+    return RSAGPU_OK;
+}
+
+int rsagpu_algo_proceed(rsagpu_algo* algo, uint64_t seed) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        set_device(algo->dom);
+        proceed(algo, seed);
+    });
+}
+
+int rsagpu_algo_reset_radgen(rsagpu_algo* algo, const rsagpu_radgen* rg) {
+    return guarded([&] {
+        if (!algo || !rg) raise(RSAGPU_ERR_ARG, "null argument");
+        // operator_algorithm.ixx:238-250
+        if (algo->rg.rmax() < rg->rmax()) raise(RSAGPU_ERR_ARG, "Incorrect maximal radius");
+        if (rg->rmin() < algo->dom->grid.rmin)
+            raise(RSAGPU_ERR_STATE, "a smaller minimal radius than the grid's needs a regrid (not built)");
+        algo->rg = *rg;
+        algo->rg.idx = 0;
+        algo->begun = false;
+    });
+}
+
+int rsagpu_algo_trace(rsagpu_algo* algo, uint64_t* voxels, uint64_t* darts, uint64_t* accepted, uint8_t* refined,
+                      int32_t* level, uint64_t cap, uint64_t* n_out) {
+    if (!algo || !n_out) return fail(RSAGPU_ERR_ARG, "null argument");
+    *n_out = algo->trace.size();
+    const uint64_t n = std::min<uint64_t>(cap, algo->trace.size());
+    for (uint64_t i = 0; i < n; i++) {
+        const TraceRow& t = algo->trace[i];
+        if (voxels) voxels[i] = t.voxels;
+        if (darts) darts[i] = t.darts;
+        if (accepted) accepted[i] = t.accepted;
+        if (refined) refined[i] = t.refined;
+        if (level) level[i] = t.level;
+    }
+    return RSAGPU_OK;
+}
+
+int rsagpu_algo_stats(rsagpu_algo* algo, rsagpu_stats* out) {
+    if (!algo || !out) return fail(RSAGPU_ERR_ARG, "null argument");
+    *out = algo->stats;
+    return RSAGPU_OK;
+}
+
+int rsagpu_algo_begin(rsagpu_algo* algo) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        set_device(algo->dom);
+        begin(algo);
+        CK(cudaStreamSynchronize(algo->stream));
+    });
+}
+
+int rsagpu_algo_replay_round(rsagpu_algo* algo, uint64_t n, const double* pos, const uint64_t* key, const double* rad,
+                             const int* phase, uint64_t max_new, int may_outreach, uint8_t* accepted_out,
+                             uint64_t* n_new) {
+    return guarded([&] {
+        if (!algo || !n_new || (n > 0 && (!pos || !key || !rad || !accepted_out)))
+            raise(RSAGPU_ERR_ARG, "null argument");
+        if (n > 0x7fffffffull) raise(RSAGPU_ERR_CAPACITY, "too many candidates");
+        set_device(algo->dom);
+        const int D = algo->dom->dim;
+        ensure_cand(algo, n);
+        reset_counters(algo);
+        *n_new = 0;
+        if (n == 0) return;
+        CandArgs c = cand_args(algo, (uint32_t)n);
+        CK(cudaMemcpyAsync(c.pos, pos, n * D * sizeof(double), cudaMemcpyHostToDevice, algo->stream));
+        CK(cudaMemcpyAsync(c.key, key, n * sizeof(uint64_t), cudaMemcpyHostToDevice, algo->stream));
+        CK(cudaMemcpyAsync(c.rad, rad, n * sizeof(double), cudaMemcpyHostToDevice, algo->stream));
+        if (phase) CK(cudaMemcpyAsync(c.phase, phase, n * sizeof(int32_t), cudaMemcpyHostToDevice, algo->stream));
+        else CK(cudaMemsetAsync(c.phase, 0, n * sizeof(int32_t), algo->stream));
+        CK(cudaMemsetAsync(c.state, ST_UNDECIDED, n, algo->stream));
+        *n_new = decide_round(algo, (uint32_t)n, max_new, may_outreach != 0, true);
+        std::vector<uint8_t> st(n);
+        CK(cudaMemcpyAsync(st.data(), c.state, n, cudaMemcpyDeviceToHost, algo->stream));
+        CK(cudaStreamSynchronize(algo->stream));
+        for (uint64_t i = 0; i < n; i++) accepted_out[i] = st[i] == ST_ACCEPTED;
+    });
+}
+
+int rsagpu_algo_end_round(rsagpu_algo* algo, uint64_t n_shots, uint64_t n_new, int* refined, int* done) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        if (!algo->begun) raise(RSAGPU_ERR_STATE, "end_round before begin");
+        set_device(algo->dom);
+        bool r = false;
+        const bool dn = end_round(algo, n_shots, n_new, &r, reference_miss_threshold(algo->dom->dim));
+        CK(cudaStreamSynchronize(algo->stream));
+        if (refined) *refined = r;
+        if (done) *done = dn;
+    });
+}
+
+int rsagpu_algo_refine(rsagpu_algo* algo) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        if (!algo->begun) raise(RSAGPU_ERR_STATE, "refine before begin");
+        set_device(algo->dom);
+        refine(algo);
+        CK(cudaStreamSynchronize(algo->stream));
+    });
+}
+
+int rsagpu_algo_voxels(rsagpu_algo* algo, int64_t* coords, uint64_t cap, uint64_t* count, int32_t* level,
+                       double* length) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        if (!algo->begun) raise(RSAGPU_ERR_STATE, "voxels before begin");
+        set_device(algo->dom);
+        const int D = algo->dom->dim;
+        if (count) *count = algo->V;
+        if (level) *level = algo->level;
+        if (length)
+            for (int d = 0; d < D; d++) length[d] = algo->len[d];
+        if (coords && cap >= algo->V && algo->V > 0) {
+            std::vector<int32_t> h(algo->V * D);
+            CK(cudaMemcpyAsync(h.data(), algo->vox[algo->cur], h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               algo->stream));
+            CK(cudaStreamSynchronize(algo->stream));
+            for (uint64_t i = 0; i < h.size(); i++) coords[i] = h[i];
+        }
+    });
+}
+
+int rsagpu_algo_draw_darts(rsagpu_algo* algo, uint64_t seed, uint64_t round, uint64_t n, double* pos, uint64_t* key,
+                           uint64_t* voxel_index) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        if (!algo->begun) raise(RSAGPU_ERR_STATE, "draw before begin");
+        if (algo->V == 0) raise(RSAGPU_ERR_STATE, "Impossible to draw centers in no voxels");
+        if (n > 0x7fffffffull) raise(RSAGPU_ERR_CAPACITY, "too many darts");
+        set_device(algo->dom);
+        const int D = algo->dom->dim;
+        ensure_cand(algo, n);
+        if (n == 0) return;
+        DartArgs da{};
+        da.n = (uint32_t)n;
+        da.V = algo->V;
+        da.vox = algo->vox[algo->cur];
+        for (int d = 0; d < D; d++) da.len[d] = algo->len[d];
+        da.seed = seed;
+        da.round = round;
+        da.radius = algo->rg.r[std::min<int>(algo->rg.idx, (int)algo->rg.r.size() - 1)];
+        da.phase = 0;
+        da.vidx_out = algo->cand.vidx;
+        CandArgs c = cand_args(algo, (uint32_t)n);
+        algo->ops->darts(algo->dom->grid.a, c, da, algo->stream);
+        if (pos) CK(cudaMemcpyAsync(pos, c.pos, n * D * sizeof(double), cudaMemcpyDeviceToHost, algo->stream));
+        if (key) CK(cudaMemcpyAsync(key, c.key, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, algo->stream));
+        if (voxel_index)
+            CK(cudaMemcpyAsync(voxel_index, algo->cand.vidx, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, algo->stream));
+        CK(cudaStreamSynchronize(algo->stream));
+    });
+}
+
+int rsagpu_batch_run(const rsagpu_instance_desc* inst, int n, uint64_t* counts_out, double* fractions_out,
+                     double* seconds_out) {
+    return fail(RSAGPU_ERR_STATE, "batch form not built yet (%p %d %p %p %p)", (const void*)inst, n, (void*)counts_out,
+                (void*)fractions_out, (void*)seconds_out);
+}
+
+int rsagpu_mlp_forward(const uint16_t* w, const float* x, uint64_t n, float* y) {
+    return fail(RSAGPU_ERR_STATE, "mlp not built yet (%p %p %llu %p)", (const void*)w, (const void*)x,
+                (unsigned long long)n, (void*)y);
+}
+
+int rsagpu_mlp_train_step(float* master, uint16_t* w, const float* x, const float* t, uint64_t n, float lr,
+                          float* loss, float* grad) {
+    return fail(RSAGPU_ERR_STATE, "mlp not built yet (%p %p %p %p %llu %f %p %p)", (void*)master, (void*)w,
+                (const void*)x, (const void*)t, (unsigned long long)n, lr, (void*)loss, (void*)grad);
+}
+
+}  // extern "C"

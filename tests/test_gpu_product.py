@@ -1,0 +1,129 @@
+"""The product path (Philox darts, GPU schedule) on the GPU: validity, maximality, statistics, and the
+dart kernel against its formula; plus replay edge cases (ties, exact contact, periodic wrap, empty)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from rsa_mpi_gb300 import _lib
+from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator
+from gpu_helpers import INDEX, sort_voxels
+
+pytestmark = pytest.mark.gpu
+
+
+def run_product(dim, L, r, seed, **sched):
+    rg = RadiusGenerator(dim, [(r, 1.0, 0)], volume=float(np.prod(L)))
+    dom = Domain([0.0] * dim, L, r)
+    algo = Algo(dom, rg, 6000)
+    if sched:
+        algo.set_schedule(**sched)
+    algo.proceed(seed)
+    return dom, algo
+
+
+@pytest.mark.parametrize("dim,L,r,phi_ref,tol", [
+    (2, [1.0, 1.0], 0.005, 0.547187, 0.006),      # config 1 (reference: 6,967 discs, 0.547187)
+    (3, [1.0, 1.0, 1.0], 0.02, 0.385201, 0.008),  # reference: 11,495 spheres, 0.38520
+    (2, [1.3, 0.7], 0.02, 0.500142 / (1.3 * 0.7) * (1.3 * 0.7), 0.03),
+])
+def test_product_run_is_valid_maximal_and_matches_fraction(dim, L, r, phi_ref, tol):
+    dom, algo = run_product(dim, L, r, 7)
+    st = algo.stats()
+    assert st["maximal"] == 1
+    pos, rad, ph = dom.arrays()
+    assert dom.check() == (0, 0)
+    inf = [0.0] * dim
+    assert O.count_overlaps(dim, inf, L, pos, rad) == 0
+    assert O.uncovered_after_refinement(dim, inf, L, pos, rad, r, r, 40) == 0
+    phi = len(rad) * O.volume_sphere(dim, r) / float(np.prod(L))
+    assert abs(dom.spheres_volume() / float(np.prod(L)) - phi) < 1e-9
+    assert abs(phi - phi_ref) < tol, (phi, phi_ref)
+
+
+def test_product_runs_are_deterministic_per_seed():
+    d1, _ = run_product(2, [1.0, 1.0], 0.01, 3)
+    d2, _ = run_product(2, [1.0, 1.0], 0.01, 3)
+    a = d1.arrays()[0]
+    b = d2.arrays()[0]
+    np.testing.assert_array_equal(a, b)
+
+
+def test_dart_kernel_follows_pick_points_formula():
+    rg = RadiusGenerator(3, [(0.02, 1.0, 0)], volume=1.0)
+    dom = Domain([0.0] * 3, [1.0, 1.0, 1.0], 0.02)
+    algo = Algo(dom, rg, 6000)
+    algo.begin()
+    vox, ln, lvl = algo.voxels()
+    pos, key, vidx = algo.draw_darts(11, 5, 4096)
+    for i in range(0, 4096, 97):
+        w = []
+        for c in range(3):
+            w += list(O.philox4x32_10([i, 5, 0, c], [11, 0]))
+        r64 = (int(w[0]) << 32) | int(w[1])
+        v = (r64 * len(vox)) >> 64
+        assert v == vidx[i]
+        for d in range(3):
+            bits = ((int(w[2 + 2 * d]) << 32) | int(w[3 + 2 * d])) >> 11
+            u = bits * 2.0 ** -53
+            orig = 0.0 + float(vox[v, d]) * ln[d]
+            assert pos[i, d] == orig + ln[d] * u
+        assert key[i] == (int(w[8]) << 32) | i
+
+
+def _fresh(dim=2, L=(1.0, 1.0), r=0.05):
+    rg = RadiusGenerator(dim, [(r, 10**9, 0)])
+    dom = Domain([0.0] * dim, list(L), r)
+    algo = Algo(dom, rg, 6000)
+    algo.begin()
+    return dom, algo
+
+
+def test_replay_edge_cases():
+    dom, algo = _fresh()
+    r = 0.05
+    # empty round
+    acc, n = algo.replay_round(np.zeros((0, 2)), np.zeros(0, np.uint64), np.zeros(0))
+    assert n == 0 and len(acc) == 0
+    # exact contact is not an overlap (dist^2 == (r1+r2)^2): both accepted
+    pos = np.array([[0.25, 0.5], [0.35, 0.5]])
+    acc, n = algo.replay_round(pos, np.array([1, 2], np.uint64) << np.uint64(32), np.full(2, r))
+    assert list(acc) == [True, True]
+    # equal priorities do not block each other (the reference's detection sees strictly smaller ones)
+    pos = np.array([[0.7, 0.2], [0.72, 0.2]])
+    acc, n = algo.replay_round(pos, np.array([5, 5], np.uint64) << np.uint64(32), np.full(2, r))
+    assert list(acc) == [True, True]
+    # a chain a < b < c with a-b and b-c overlapping: a and c accepted, b rejected
+    pos = np.array([[0.5, 0.85], [0.58, 0.85], [0.66, 0.85]])
+    acc, n = algo.replay_round(pos, np.array([1, 2, 3], np.uint64) << np.uint64(32), np.full(3, r))
+    assert list(acc) == [True, False, True]
+    # periodic wrap: a candidate near x = 1 overlaps a sphere near x = 0
+    pos = np.array([[0.02, 0.05]])
+    acc, _ = algo.replay_round(pos, np.array([1], np.uint64), np.full(1, r))
+    assert list(acc) == [True]
+    pos = np.array([[0.95, 0.05], [0.99, 0.99]])
+    acc, _ = algo.replay_round(pos, np.array([1, 2], np.uint64), np.full(2, r))
+    assert list(acc) == [False, False]
+    assert dom.check() == (0, 0)
+
+
+def test_replay_matches_oracle_on_random_dense_batches():
+    """Large random batches with heavy in-batch conflicts and repeated priorities."""
+    rng = np.random.default_rng(5)
+    for dim, L, r in ((2, [1.0, 1.0], 0.01), (3, [1.0, 0.8, 0.6], 0.03)):
+        ora = O.Oracle(dim, [0.0] * dim, L, [(r, 10**9, 0)], counts=True)
+        rg = RadiusGenerator(dim, [(r, 10**9, 0)])
+        dom = Domain([0.0] * dim, L, r)
+        algo = Algo(dom, rg, 6000)
+        ora.begin(0)
+        algo.begin()
+        for rnd in range(4):
+            n = 20000
+            pos = rng.random((n, dim)) * np.array(L)
+            key = rng.integers(0, 2**14, n).astype(np.uint64)  # many ties
+            rad = np.full(n, r)
+            acc_o, n_o = ora.apply_round(pos, key, rad, np.zeros(n, np.int32))
+            acc_g, n_g = algo.replay_round(pos, key << np.uint64(32), rad)
+            assert n_o == n_g and np.array_equal(acc_o, acc_g)
+        algo.refine()
+        ora.refine()
+        np.testing.assert_array_equal(sort_voxels(ora.voxels()[0]), sort_voxels(algo.voxels()[0]))
