@@ -1,0 +1,330 @@
+"""Benchmark: spheres/s to certified maximality on one GB300 (and N replicas for N GPUs).
+
+Workload (one step): the 3D periodic unit cube, monodisperse r = 0.002, seed 1, sampled to certified
+maximality (no uncovered voxel left) by the plain FP64 GPU form -- about 11.5 M spheres.  Inputs are
+the configuration only; the working set (sphere grid 434^3 cells, voxel lists of 10^8+ entries) is far
+larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
+
+value  = spheres placed / device time of proceed() (CUDA events on the sampler's stream), summed over
+         ranks, divided by the max over ranks.
+e2e    = the same metric through the C ABI as a user calls it: create domain + algo, proceed, copy the
+         spheres (centres, radii, phases) to host buffers, destroy; timed on the host clock.
+roofline: the refinement mask kernel (the dominant kernel), algorithmic bytes / its CUDA-event time,
+         against the measured HBM copy bandwidth of this GPU.
+cpu_baseline: the oracle's C restatement of the reference (single thread) on a bounded sample of the
+         same workload (same radius, periodic box of side 0.2 = 1/125 of the volume).
+--impl reference: the CPU path of the reference, restated by the oracle (the reference itself cannot
+         be compiled on the GPU host, which has no copy of its sources): one instance per host core on
+         the bounded sample, run concurrently; the line reports their aggregate spheres/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "spheres/s to certified maximality"
+WORKLOADS = {
+    # name: (dim, L, r, seed, description)
+    "config2": (3, [1.0, 1.0, 1.0], 0.002, 1, "3D periodic unit cube, r=0.002, seed 1, to certified maximality"),
+    "3d_r0.004": (3, [1.0, 1.0, 1.0], 0.004, 1, "3D periodic unit cube, r=0.004, seed 1, to certified maximality"),
+    "config1": (2, [1.0, 1.0], 0.005, 0, "2D periodic unit square, r=0.005, seed 0, to certified maximality"),
+}
+CPU_SAMPLE = (3, [0.2, 0.2, 0.2], 0.002, 1)
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.strip().split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip() == "Active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_gpu_step(dim, L, r, seed, form=0):
+    from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator
+    rg = RadiusGenerator(dim, [(r, 1.0, 0)], volume=float(math.prod(L)))
+    dom = Domain([0.0] * dim, L, r)
+    algo = Algo(dom, rg, 6000)
+    algo.set_form(form)
+    algo.proceed(seed)
+    st = algo.stats()
+    ms, by = algo.kernel_profile()
+    n = dom.count()
+    algo.close()
+    dom.close()
+    return n, st, ms, by
+
+
+def run_e2e_step(dim, L, r, seed):
+    """The user's call through the C ABI with host buffers: returns (spheres, seconds, d2h bytes, h2d bytes)."""
+    import ctypes as C
+    import numpy as np
+    from rsa_mpi_gb300 import _lib
+    Lb = _lib.lib()
+    t0 = time.perf_counter()
+    inf = np.zeros(dim)
+    sup = np.asarray(L, dtype=np.float64)
+    dom = C.c_void_p()
+    _lib.check(Lb.rsagpu_domain_create(dim, _lib.ptr(inf, _lib._d), _lib.ptr(sup, _lib._d), r, C.byref(dom)))
+    rr = np.array([r])
+    phi = np.array([1.0])
+    ph = np.zeros(1, np.int32)
+    rg = C.c_void_p()
+    _lib.check(Lb.rsagpu_radgen_create_fractions(dim, _lib.ptr(rr, _lib._d), _lib.ptr(phi, _lib._d), _lib.ptr(ph, _lib._i32),
+                                                 1, float(np.prod(sup)), 0.0, C.byref(rg)))
+    algo = C.c_void_p()
+    _lib.check(Lb.rsagpu_algo_create(dom, rg, 6000, C.byref(algo)))
+    _lib.check(Lb.rsagpu_algo_proceed(algo, seed))
+    n = C.c_uint64()
+    _lib.check(Lb.rsagpu_domain_extract(dom, None, None, None, 0, C.byref(n)))
+    k = n.value
+    pos = np.empty((k, dim))
+    rad = np.empty(k)
+    phs = np.empty(k, np.int32)
+    _lib.check(Lb.rsagpu_domain_extract(dom, _lib.ptr(pos, _lib._d), _lib.ptr(rad, _lib._d), _lib.ptr(phs, _lib._i32), k,
+                                        C.byref(n)))
+    Lb.rsagpu_algo_destroy(algo)
+    Lb.rsagpu_radgen_destroy(rg)
+    Lb.rsagpu_domain_destroy(dom)
+    t1 = time.perf_counter()
+    return k, t1 - t0, pos.nbytes + rad.nbytes + phs.nbytes
+
+
+def cpu_sample(dim, L, r, seed):
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    o = O.Oracle(dim, [0.0] * dim, L, [(r, 1.0, 0)])
+    o.proceed(seed)
+    n = len(o.spheres()[1])
+    return n, time.perf_counter() - t0
+
+
+def _cpu_worker(args):
+    dim, L, r, seed = args
+    return cpu_sample(dim, L, r, seed)
+
+
+def reference_arm(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    dim, L, r, seed = CPU_SAMPLE
+    ctx = mp.get_context("spawn")
+    vals = []
+    with ctx.Pool(cores) as pool:
+        for _ in range(1 if args.warmup > 0 else 0):
+            pool.map(_cpu_worker, [(dim, L, r, seed + i) for i in range(cores)])
+        step_ms = []
+        for s in range(args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_worker, [(dim, L, r, seed + 1000 * s + i) for i in range(cores)])
+            el = time.perf_counter() - t0
+            vals.append(sum(n for n, _ in res) / el)
+            step_ms.append(el * 1e3)
+    value = statistics.median(vals)
+    wl = WORKLOADS[args.workload]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "spheres/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(step_ms),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl[4], "cpu_sample": "3D periodic box of side 0.2 (1/125 of the unit cube), r=0.002, "
+                   f"one instance per core ({cores}), seeds 1000*step+i"},
+        "cpu_baseline": {"value": value, "unit": "spheres/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} concurrent instances of the 3D box-0.2 r=0.002 case"},
+        "e2e": {"value": value, "unit": "spheres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    rank, world, local = env_rank()
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from rsa_mpi_gb300 import build as B
+    B.build()
+    from rsa_mpi_gb300.sampler import kernel_launches
+
+    dim, L, r, seed0, desc = WORKLOADS[args.workload]
+    seed = seed0 + rank  # each rank samples an independent instance (replicas)
+    for _ in range(args.warmup):
+        run_gpu_step(dim, L, r, seed)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    launches0 = kernel_launches()
+    barrier()
+    spheres, dev_ms, wall = 0, 0.0, 0.0
+    mask_ms, mask_bytes = [], []
+    stats = None
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            n, st, ms, by = run_gpu_step(dim, L, r, seed)
+            spheres += n
+            dev_ms += st["ms_total"]
+            mask_ms += list(ms)
+            mask_bytes += list(by)
+            stats = st
+        barrier()
+        wall = time.perf_counter() - t0
+    launches = kernel_launches() - launches0
+
+    # e2e through the C ABI with host buffers
+    e2e_n, e2e_s, d2h = 0, 0.0, 0
+    for _ in range(max(1, args.steps)):
+        k, s, b = run_e2e_step(dim, L, r, seed)
+        e2e_n += k
+        e2e_s += s
+        d2h = b
+    t = torch.tensor([dev_ms, wall, e2e_s], dtype=torch.float64, device="cuda")
+    tot = torch.tensor([float(spheres), float(e2e_n)], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+    dev_ms_max, wall_max, e2e_max = t.tolist()
+    spheres_all, e2e_all = tot.tolist()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    peak, peak_kind = measured_peaks()
+    import numpy as np
+    mm = np.asarray(mask_ms)
+    mb = np.asarray(mask_bytes)
+    achieved = float(mb.sum() / (mm.sum() * 1e-3) / 1e9) if mm.sum() > 0 else 0.0
+    traffic_path = os.path.join(ROOT, "profiles", "refine_mask_traffic.json")
+    traffic = None
+    if os.path.exists(traffic_path):
+        try:
+            traffic = json.load(open(traffic_path)).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC,
+        "value": spheres_all / (dev_ms_max * 1e-3),
+        "unit": "spheres/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": desc, "form": "plain FP64", "spheres_per_step": spheres // max(1, args.steps),
+                   "parallelism": f"replicas x{world}", "l2": "working set > L2 (no flush needed)"},
+        "wall_ms_per_step": wall_max * 1e3 / args.steps,
+        "roofline": {"bound": "hbm", "kernel": "k_refine_mask", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "share_of_step": float(mm.sum() / max(dev_ms, 1e-9)),
+                     "launches": int(len(mm)), "algorithmic_bytes_per_launch": float(mb.mean()) if len(mb) else 0.0},
+        "e2e": {"value": e2e_all / e2e_max, "unit": "spheres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "stats": {k: stats[k] for k in ("rounds", "refinements", "darts", "settle_iterations", "peak_voxels", "final_level",
+                                         "maximal")},
+    }
+    cs = clocks.summary()
+    if cs:
+        line["clocks"] = cs
+    if not args.no_cpu_baseline:
+        n, s = cpu_sample(*CPU_SAMPLE)
+        line["cpu_baseline"] = {"value": n / s, "unit": "spheres/s", "cores": 1, "kind": "port",
+                                "sample": "3D periodic box of side 0.2 (1/125 of the unit cube), r=0.002, seed 1, "
+                                          f"to certified maximality: {n} spheres in {s:.1f} s"}
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

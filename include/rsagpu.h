@@ -132,6 +132,10 @@ typedef struct {
     int32_t final_level, maximal;
 } rsagpu_stats;
 int rsagpu_algo_stats(rsagpu_algo* algo, rsagpu_stats* out);
+/* Per launch of the refinement's mask kernel in the last proceed(): device milliseconds (CUDA events
+ * on the algo's stream around the launch) and algorithmic bytes (parent coordinates, stencil occupancy
+ * bits up to the grid size, visited spheres up to the spheres placed, child masks). */
+int rsagpu_algo_kernel_profile(rsagpu_algo* algo, double* ms, double* bytes, uint64_t cap, uint64_t* n_out);
 /* Turns per-kernel CUDA-event timing on (1) or off (0, default). */
 int rsagpu_algo_set_timing(rsagpu_algo* algo, int on);
 

@@ -317,6 +317,21 @@ static void store_init(ora_store* s, int D, const double* inf, const double* L, 
     for (int64_t i = 0; i < s->ncells; i++) s->head[i] = -1;
 }
 
+/* an empty store with the same cells as *like */
+static void store_init_like(ora_store* s, const ora_store* like) {
+    memset(s, 0, sizeof(*s));
+    s->D = like->D;
+    s->ncells = like->ncells;
+    for (int d = 0; d < like->D; d++) {
+        s->inf[d] = like->inf[d];
+        s->L[d] = like->L[d];
+        s->n[d] = like->n[d];
+        s->c[d] = like->c[d];
+    }
+    s->head = (int64_t*)malloc(sizeof(int64_t) * s->ncells);
+    for (int64_t i = 0; i < s->ncells; i++) s->head[i] = -1;
+}
+
 static void store_free(ora_store* s) {
     free(s->head); free(s->pos); free(s->rad); free(s->phase); free(s->key); free(s->next);
     memset(s, 0, sizeof(*s));
@@ -798,6 +813,7 @@ typedef struct {
     uint64_t key;
     const uint64_t* ids; /* store slot -> candidate index */
     const int8_t* status;
+    uint64_t self;
     int blocked_real_u, blocked_conflict;
 } pass_ctx;
 
@@ -805,7 +821,8 @@ enum { ST_NONE = 0, ST_U = 1, ST_C = 2, ST_S = 3 };
 
 static int pass_visit(void* vctx, uint64_t slot, const double* img) {
     pass_ctx* c = (pass_ctx*)vctx;
-    if (!(c->keys[slot] < c->key)) return 0;
+    const uint64_t other = c->ids[slot];
+    if (!(c->keys[slot] < c->key || (c->keys[slot] == c->key && other < c->self))) return 0;
     if (!ora_collide(c->D, c->r, c->x, c->rads[slot], img)) return 0;
     int wrapped = 0;
     for (int d = 0; d < c->D; d++) wrapped |= (img[d] != c->pos[slot * c->D + d]);
@@ -825,8 +842,7 @@ static void pass_classify(const rsa_oracle* o, const uint64_t* und, uint64_t nu,
     const uint64_t* key, const double* rad, int8_t* status) {
     const int D = o->D;
     ora_store tmp;
-    store_init(&tmp, D, o->inf, o->L, o->st.c[0]);
-    for (int d = 0; d < D; d++) { tmp.n[d] = o->st.n[d]; tmp.c[d] = o->st.c[d]; }
+    store_init_like(&tmp, &o->st);
     uint64_t* ids = (uint64_t*)malloc(sizeof(uint64_t) * (nu ? nu : 1));
     for (uint64_t t = 0; t < nu; t++) {
         store_add(&tmp, pos + und[t] * D, rad[und[t]], 0, key[und[t]]);
@@ -834,7 +850,7 @@ static void pass_classify(const rsa_oracle* o, const uint64_t* und, uint64_t nu,
     }
     for (uint64_t t = 0; t < nu; t++) {
         uint64_t i = und[t];
-        pass_ctx c = { D, pos + i * D, rad[i], tmp.pos, tmp.rad, tmp.key, key[i], ids, status, 0, 0 };
+        pass_ctx c = { D, pos + i * D, rad[i], tmp.pos, tmp.rad, tmp.key, key[i], ids, status, i, 0, 0 };
         store_visit(&tmp, pos + i * D, pass_visit, &c);
         status[i] = c.blocked_conflict ? ST_C : (c.blocked_real_u ? ST_S : ST_U);
     }
@@ -912,9 +928,11 @@ static int apply_capped(rsa_oracle* o, uint64_t n, const double* pos, const uint
 
 /* Decisions of generate_spheres (operator_algorithm.ixx:534-566): a candidate is accepted iff
  * it overlaps no validated sphere (remove_collisions_with_validated_spheres,
- * operator_cells_and_data_storage.ixx:54-76) and no accepted candidate of strictly smaller
- * priority (find_solve_conflicts + the add_to_sample loop, :79-143 and
- * operator_algorithm.ixx:383-443).  When the round may exceed the class count
+ * operator_cells_and_data_storage.ixx:54-76) and no accepted candidate that precedes it in
+ * (priority, candidate index) order (find_solve_conflicts + the add_to_sample loop, :79-143 and
+ * operator_algorithm.ixx:383-443).  The reference's detection sees strictly smaller priorities
+ * only (:39), so it accepts two overlapping candidates of equal priority; the index breaks
+ * that tie instead.  When the round may exceed the class count
  * (may_outreach), only the max_new accepted candidates of smallest priority are kept
  * (retain_only_first_elements, operator_algorithm.ixx:475-519). */
 int ora_apply_round(rsa_oracle* o, uint64_t n, const double* pos, const uint64_t* key,
@@ -939,17 +957,14 @@ int ora_apply_round(rsa_oracle* o, uint64_t n, const double* pos, const uint64_t
     qsort(order, n, sizeof(uint64_t), cmp_key_idx);
     /* accepted candidates in a scratch store, in priority order */
     ora_store acc; /* same cells as the main store */
-    store_init(&acc, D, o->inf, o->L, o->st.c[0]);
-    for (int d = 0; d < D; d++) {
-        acc.n[d] = o->st.n[d];
-        acc.c[d] = o->st.c[d];
-    }
+    store_init_like(&acc, &o->st);
     uint64_t* acc_ids = (uint64_t*)malloc(sizeof(uint64_t) * (n ? n : 1));
     uint64_t nacc = 0;
     for (uint64_t t = 0; t < n; t++) {
         uint64_t i = order[t];
         if (!alive[i]) continue;
-        hit_ctx c = { D, pos + i * D, rad[i], acc.rad, acc.key, key[i], 1, 0 };
+        /* every candidate in acc precedes i in (key, index) order, so any overlap blocks i */
+        hit_ctx c = { D, pos + i * D, rad[i], acc.rad, acc.key, key[i], 0, 0 };
         store_visit(&acc, pos + i * D, hit_visit, &c);
         if (!c.hit) {
             store_add(&acc, pos + i * D, rad[i], phase[i], key[i]);

@@ -61,8 +61,10 @@ const uint64_t* ora_cand_key(const rsa_oracle* o);   /* priority (31-bit) */
 const double* ora_cand_rad(const rsa_oracle* o);
 const int* ora_cand_phase(const rsa_oracle* o);
 /* Decides a batch of candidates against the validated set and among themselves, inserts the
- * accepted ones.  accepted_out[i] = 1 if candidate i is accepted.  key ties do not block
- * (detection sees strictly smaller priorities only, operator_cells_and_data_storage.ixx:39). */
+ * accepted ones.  accepted_out[i] = 1 if candidate i is accepted.  Candidates are ordered by
+ * (key, index): equal keys are broken by the candidate index (the reference's detection sees
+ * strictly smaller priorities only, operator_cells_and_data_storage.ixx:39, and so accepts both
+ * of two overlapping equal-priority candidates). */
 int ora_apply_round(rsa_oracle* o, uint64_t n, const double* pos, const uint64_t* key,
     const double* rad, const int* phase, uint64_t max_new, int may_outreach,
     uint8_t* accepted_out, uint64_t* n_new);

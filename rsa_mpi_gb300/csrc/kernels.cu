@@ -71,13 +71,13 @@ struct NVox {
     int64_t n[D];
 };
 
-__global__ void k_vox_init(int32_t* vox, uint64_t V, NVox nv) {
+__global__ void k_vox_init(int64_t* vox, uint64_t V, NVox nv) {
     const uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     uint64_t r = v;
 #pragma unroll
     for (int d = 0; d < D; d++) {
-        vox[v * D + d] = (int32_t)(r % (uint64_t)nv.n[d]);
+        vox[v * D + d] = (int64_t)(r % (uint64_t)nv.n[d]);
         r /= (uint64_t)nv.n[d];
     }
 }
@@ -89,7 +89,7 @@ __global__ void k_vox_init(int32_t* vox, uint64_t V, NVox nv) {
 struct DartParams {
     uint32_t n;
     uint64_t V;
-    const int32_t* vox;
+    const int64_t* vox;
     double len[D];
     double inf[D];
     uint32_t seed_lo, seed_hi, round_lo, round_hi;
@@ -182,6 +182,12 @@ __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>&
     }
 }
 
+// candidate order: priority key, then candidate index (a strict total order; the reference's
+// detection compares priorities only, so two overlapping equal-priority candidates both pass there)
+__device__ __forceinline__ bool precedes(uint64_t kj, int32_t j, uint64_t ki, uint32_t i) {
+    return kj < ki || (kj == ki && (uint32_t)j < i);
+}
+
 __device__ __forceinline__ uint8_t load_state(const uint8_t* s, int32_t j) {
     return *((volatile const uint8_t*)(s + j));
 }
@@ -189,7 +195,7 @@ __device__ __forceinline__ uint8_t load_state(const uint8_t* s, int32_t j) {
 // ------------------------------------------------------------------------------------------------
 // settle: the accepted set is the sequential greedy in ascending key (find_solve_conflicts and the
 // add_to_sample loop, operator_cells_and_data_storage.ixx:79-143, operator_algorithm.ixx:383-443):
-// a candidate is accepted iff no accepted candidate of strictly smaller key overlaps it.  Computed as
+// a candidate is accepted iff no accepted candidate that precedes it (key, then index) overlaps it.  Computed as
 // a monotone fixpoint: collect stores each candidate's strictly-lower overlapping candidates (seen
 // from the candidate itself, i.e. against their periodic image); settle iterations then accept a
 // candidate whose blockers are all rejected and reject one with an accepted blocker.  The smallest
@@ -210,7 +216,7 @@ __global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
         cell_of<D>(g, geo, x, k);
         int nb = 0;
         visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
-            if (!(c.key[j] < key)) return false;
+            if (!precedes(c.key[j], j, key, i)) return false;
             if (!collide64<D>(r, x, c.rad[j], img)) return false;
             if (nb < NB) c.blk[(uint64_t)i * NB + nb] = j;
             nb++;
@@ -252,7 +258,7 @@ __global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
                 int32_t k[D];
                 cell_of<D>(g, geo, x, k);
                 visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
-                    if (!(c.key[j] < key)) return false;
+                    if (!precedes(c.key[j], j, key, i)) return false;
                     if (!collide64<D>(r, x, c.rad[j], img)) return false;
                     const uint8_t s = load_state(c.state, j);
                     any_acc |= (s == ST_ACCEPTED);
@@ -329,13 +335,15 @@ __global__ void k_commit(Grid<D> g, CandArgs c) {
 // ------------------------------------------------------------------------------------------------
 struct RefineParams {
     uint64_t V;
-    const int32_t* vin;
-    int32_t* vout;
+    const int64_t* vin;
+    int64_t* vout;
     double len[D];
     double nlen[D];
     double inf[D];
     double rmin;
     uint32_t* masks;
+    uint32_t* survivors;
+    unsigned long long* visits;
     uint32_t* block_counts;
     const uint64_t* block_offsets;
     uint32_t* err;
@@ -346,8 +354,10 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
     uint32_t mask[MASK_WORDS];
 #pragma unroll
     for (int w = 0; w < MASK_WORDS; w++) mask[w] = 0;
+    bool survived = false;
+    uint32_t visits = 0;
     if (v < p.V) {
-        int32_t cc[D];
+        int64_t cc[D];
         double orig[D], centre[D];
 #pragma unroll
         for (int d = 0; d < D; d++) {
@@ -363,6 +373,7 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
         int npre = 0;
         bool overflow = false;
         const bool covered = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
+            visits++;
             const double R = __dadd_rn(rs, p.rmin);
             const double R2 = __dmul_rn(R, R);
             if (!(maxcorner_dist2<D>(img, orig, p.len) > R2)) return true;  // parent fully covered
@@ -378,6 +389,7 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
             }
             return false;
         });
+        survived = !covered;
         if (!covered) {
             if (overflow) atomicOr(p.err, (uint32_t)ERR_PREFILTER_OVERFLOW);
             for (int t = 0; t < CHILDREN; t++) {
@@ -404,6 +416,12 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
     uint32_t cnt = 0;
 #pragma unroll
     for (int w = 0; w < MASK_WORDS; w++) cnt += __popc(mask[w]);
+    const uint32_t alive = __ballot_sync(0xffffffffu, survived);
+    if ((threadIdx.x & 31) == 0 && alive) atomicAdd(p.survivors, (uint32_t)__popc(alive));
+    uint32_t wv = visits;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wv += __shfl_xor_sync(0xffffffffu, wv, o);
+    if ((threadIdx.x & 31) == 0 && wv) atomicAdd(p.visits, (unsigned long long)wv);
     uint32_t total;
     block_exclusive_scan<REFINE_BLOCK>(cnt, &total);
     if (threadIdx.x == 0) p.block_counts[blockIdx.x] = total;
@@ -421,7 +439,7 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
     const uint32_t local = block_exclusive_scan<REFINE_BLOCK>(cnt, nullptr);
     if (v >= p.V || cnt == 0) return;
     uint64_t o = p.block_offsets[blockIdx.x] + local;
-    int32_t cc[D];
+    int64_t cc[D];
 #pragma unroll
     for (int d = 0; d < D; d++) cc[d] = p.vin[v * D + d];
     for (int t = 0; t < CHILDREN; t++) {
@@ -512,7 +530,7 @@ __global__ void __launch_bounds__(OCC_BLOCK) k_extract_write(Grid<D> g, const ui
 // ------------------------------------------------------------------------------------------------
 // host launchers
 // ------------------------------------------------------------------------------------------------
-void op_vox_init(int32_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s) {
+void op_vox_init(int64_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s) {
     NVox nv;
     for (int d = 0; d < D; d++) nv.n[d] = nvox[d];
     if (V == 0) return;
@@ -597,6 +615,8 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
     p.block_counts = a.block_counts;
     p.block_offsets = a.block_offsets;
     p.err = a.err;
+    p.survivors = a.survivors;
+    p.visits = a.visits;
     return p;
 }
 

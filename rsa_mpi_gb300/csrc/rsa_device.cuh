@@ -5,7 +5,7 @@
 //                  most one accepted centre.  occ = 1 bit per cell (10 MB for 434^3 cells, L2
 //                  resident); pos = D doubles per cell, rad = 1 double per cell, phase = int32 per
 //                  cell (all indexed by the cell, so the cell index IS the sphere id).
-//   voxel list   : AoS int32[V][D] integer coordinates at the current level, one length per level.
+//   voxel list   : AoS int64[V][D] integer coordinates at the current level, one length per level.
 //   candidates   : SoA per round (pos, key, rad, phase, cell, state, next) + a per-cell list head.
 //
 // Every FP64 decision uses __dadd_rn / __dsub_rn / __dmul_rn in the operation order of the

@@ -45,7 +45,7 @@ struct CandArgs {
 struct DartArgs {
     uint32_t n;
     uint64_t V;
-    const int32_t* vox;
+    const int64_t* vox;
     double len[MAX_D];
     uint64_t seed;
     uint64_t round;
@@ -56,8 +56,8 @@ struct DartArgs {
 
 struct RefineArgs {
     uint64_t V;
-    const int32_t* vin;
-    int32_t* vout;
+    const int64_t* vin;
+    int64_t* vout;
     double len[MAX_D];   // parent length
     double nlen[MAX_D];  // child length = 0.5 * parent
     double rmin;
@@ -65,11 +65,13 @@ struct RefineArgs {
     uint32_t* block_counts;
     uint64_t* block_offsets;
     uint32_t* err;
+    uint32_t* survivors;  // parents not covered (remove_covered keeps them)
+    unsigned long long* visits;  // occupied stencil cells visited by the mask pass
 };
 
 struct DimOps {
     int D;
-    void (*vox_init)(int32_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s);
+    void (*vox_init)(int64_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s);
     void (*darts)(const GridArgs& g, const CandArgs& c, const DartArgs& a, cudaStream_t s);
     void (*probe)(const GridArgs& g, const CandArgs& c, cudaStream_t s);
     void (*collect)(const GridArgs& g, const CandArgs& c, cudaStream_t s);

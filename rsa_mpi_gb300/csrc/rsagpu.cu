@@ -200,7 +200,7 @@ struct rsagpu_algo {
     const DimOps* ops = nullptr;
     cudaStream_t stream = nullptr;
     // voxels
-    int32_t* vox[2] = {nullptr, nullptr};
+    int64_t* vox[2] = {nullptr, nullptr};
     uint64_t vox_cap[2] = {0, 0};
     int cur = 0;
     uint64_t V = 0;
@@ -213,6 +213,9 @@ struct rsagpu_algo {
     uint64_t* block_offsets = nullptr;
     uint64_t blocks_cap = 0;
     uint32_t* d_err = nullptr;
+    unsigned long long* d_visits = nullptr;
+    uint64_t placed = 0;              // spheres in the grid
+    std::vector<double> mask_ms, mask_bytes;  // per refine_mask launch
     // candidates
     CandBuffers cand;
     uint32_t* h_counters = nullptr;  // pinned mirror: COUNTERS + MAX_SETTLE + 1
@@ -223,11 +226,12 @@ struct rsagpu_algo {
     std::vector<uint16_t> mlp;
     // state
     bool begun = false;
+    bool heads_dirty = false;  // a round stopped before its commit cleared the candidate lists
     uint64_t seed = 0, round = 0;
     std::vector<TraceRow> trace;
     rsagpu_stats stats{};
     bool timing = false;
-    cudaEvent_t ev[12]{};
+    cudaEvent_t ev[12]{};  // [8], [9] bracket the refine_mask launch
     ~rsagpu_algo() {
         cand.release();
         dfree(vox[0]);
@@ -236,6 +240,7 @@ struct rsagpu_algo {
         dfree(block_counts);
         dfree(block_offsets);
         dfree(d_err);
+        dfree(d_visits);
         if (h_counters) cudaFreeHost(h_counters);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
@@ -371,7 +376,7 @@ void ensure_vox(rsagpu_algo* A, int which, uint64_t n) {
     if (n <= A->vox_cap[which]) return;
     uint64_t cap = std::max<uint64_t>(n, A->vox_cap[which] + A->vox_cap[which] / 2);
     dfree(A->vox[which]);
-    A->vox[which] = dalloc<int32_t>(cap * D);
+    A->vox[which] = dalloc<int64_t>(cap * D);
     A->vox_cap[which] = cap;
 }
 
@@ -415,6 +420,8 @@ void begin(rsagpu_algo* A) {
     A->trace.clear();
     A->stats = rsagpu_stats{};
     A->stats.peak_voxels = V;
+    A->mask_ms.clear();
+    A->mask_bytes.clear();
 }
 
 // remove_covered + subdivide_uncovered (list_of_voxels.ixx:30-100)
@@ -422,8 +429,8 @@ void refine(rsagpu_algo* A) {
     const int D = A->dom->dim;
     if (A->V == 0) return;
     for (int d = 0; d < D; d++)
-        if ((double)A->nvox0[d] * std::ldexp(1.0, A->level + 1) > 2147483647.0)
-            raise(RSAGPU_ERR_CAPACITY, "voxel coordinates overflow int32 at level %d", A->level + 1);
+        if ((double)A->nvox0[d] * std::ldexp(1.0, A->level + 1) > 4.0e18)
+            raise(RSAGPU_ERR_CAPACITY, "voxel coordinates overflow int64 at level %d", A->level + 1);
     ensure_refine_buffers(A, A->V);
     RefineArgs r{};
     r.V = A->V;
@@ -437,12 +444,42 @@ void refine(rsagpu_algo* A) {
     r.block_counts = A->block_counts;
     r.block_offsets = A->block_offsets;
     r.err = A->d_err;
+    r.survivors = A->d_err + 1;
+    r.visits = A->d_visits;
+    CK(cudaMemsetAsync(r.survivors, 0, sizeof(uint32_t), A->stream));
+    CK(cudaMemsetAsync(r.visits, 0, sizeof(unsigned long long), A->stream));
     const uint64_t nb = (A->V + REFINE_BLOCK - 1) / REFINE_BLOCK;
+    CK(cudaEventRecord(A->ev[8], A->stream));
     A->ops->refine_mask(A->dom->grid.a, r, A->stream);
+    CK(cudaEventRecord(A->ev[9], A->stream));
     launch_scan_blocks(A->block_counts, A->block_offsets, nb, nullptr, A->stream);
     uint64_t total = 0;
+    uint32_t survivors = 0;
+    unsigned long long visits = 0;
     CK(cudaMemcpyAsync(&total, A->block_offsets + nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, A->stream));
+    CK(cudaMemcpyAsync(&survivors, r.survivors, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
+    CK(cudaMemcpyAsync(&visits, r.visits, sizeof(unsigned long long), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaStreamSynchronize(A->stream));
+    {
+        // the mask pass of this launch: its device time and algorithmic bytes (each logical element once:
+        // parent coordinates, stencil occupancy bits up to the grid size, visited spheres up to the
+        // spheres placed, the child masks)
+        float ms = 0;
+        cudaEventElapsedTime(&ms, A->ev[8], A->ev[9]);
+        const GridArgs& g = A->dom->grid.a;
+        const double bits = std::min<double>((double)A->V * g.S, (double)g.ncells);
+        const double sph = std::min<double>((double)visits, (double)A->placed);
+        A->mask_ms.push_back(ms);
+        A->mask_bytes.push_back((double)A->V * 8 * D + bits / 8 + sph * (8.0 * D + 8) +
+                                (double)A->V * 4 * A->ops->mask_words);
+    }
+    if (survivors == 0) {
+        // remove_covered emptied the list: subdivide_uncovered returns before halving the length
+        // (list_of_voxels.ixx:58)
+        A->V = 0;
+        A->stats.refinements++;
+        return;
+    }
     const int other = 1 - A->cur;
     ensure_vox(A, other, total);
     r.vout = A->vox[other];
@@ -515,6 +552,12 @@ float ev_ms(rsagpu_algo* A, int a, int b) {
 uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_outreach, bool keep_state) {
     rsagpu_domain* dom = A->dom;
     const GridArgs& g = dom->grid.a;
+    if (A->heads_dirty) {
+        // stale list heads would link this round's candidates to indices of an unfinished round
+        CK(cudaMemsetAsync(dom->grid.head, 0xFF, g.ncells * sizeof(int32_t), A->stream));
+        A->heads_dirty = false;
+    }
+    A->heads_dirty = true;
     CandArgs c = cand_args(A, n);
     const DimOps* ops = A->ops;
     ev_record(A, 2);
@@ -570,12 +613,14 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
         }
     }
     ops->commit(g, c, A->stream);
+    A->heads_dirty = false;
     ev_record(A, 5);
     CK(cudaMemcpyAsync(A->h_counters, c.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaStreamSynchronize(A->stream));
     if (A->h_counters[2] & ERR_DOUBLE_OCCUPANCY)
         raise(RSAGPU_ERR_INVARIANT, "two accepted centres in one grid cell");
     (void)keep_state;
+    A->placed += A->h_counters[1];
     if (A->timing) {
         A->stats.ms_probe += ev_ms(A, 2, 3);
         A->stats.ms_settle += ev_ms(A, 3, 4);
@@ -930,10 +975,12 @@ int rsagpu_algo_create(rsagpu_domain* dom, const rsagpu_radgen* rg, int nbshots,
             if (!A->ops) raise(RSAGPU_ERR_ARG, "dimension not built");
             CK(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking));
             for (auto& e : A->ev) CK(cudaEventCreate(&e));
-            A->d_err = dalloc<uint32_t>(1);
-            CK(cudaMemset(A->d_err, 0, sizeof(uint32_t)));
+            A->d_err = dalloc<uint32_t>(2);
+            CK(cudaMemset(A->d_err, 0, 2 * sizeof(uint32_t)));
+            A->d_visits = dalloc<unsigned long long>(1);
             // the algo rebuilds the domain's grid and drops its spheres (operator_algorithm.ixx:25-26)
             build_grid(dom, rg->rmin(), std::max(rg->rmax(), 0.0));
+            A->placed = 0;
             ensure_cand(A, 1024);
         } catch (...) {
             delete A;
@@ -988,6 +1035,16 @@ int rsagpu_algo_set_mlp(rsagpu_algo* algo, const uint16_t* w, uint64_t n) {
         if (n != 5378) raise(RSAGPU_ERR_ARG, "expected 5378 weights, got %llu", (unsigned long long)n);
         algo->mlp.assign(w, w + n);
     });
+}
+
+int rsagpu_algo_kernel_profile(rsagpu_algo* algo, double* ms, double* bytes, uint64_t cap, uint64_t* n_out) {
+    if (!algo || !n_out) return fail(RSAGPU_ERR_ARG, "null argument");
+    *n_out = algo->mask_ms.size();
+    for (uint64_t i = 0; i < std::min<uint64_t>(cap, algo->mask_ms.size()); i++) {
+        if (ms) ms[i] = algo->mask_ms[i];
+        if (bytes) bytes[i] = algo->mask_bytes[i];
+    }
+    return RSAGPU_OK;
 }
 
 int rsagpu_algo_set_timing(rsagpu_algo* algo, int on) {
@@ -1111,11 +1168,9 @@ int rsagpu_algo_voxels(rsagpu_algo* algo, int64_t* coords, uint64_t cap, uint64_
         if (length)
             for (int d = 0; d < D; d++) length[d] = algo->len[d];
         if (coords && cap >= algo->V && algo->V > 0) {
-            std::vector<int32_t> h(algo->V * D);
-            CK(cudaMemcpyAsync(h.data(), algo->vox[algo->cur], h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost,
+            CK(cudaMemcpyAsync(coords, algo->vox[algo->cur], algo->V * D * sizeof(int64_t), cudaMemcpyDeviceToHost,
                                algo->stream));
             CK(cudaStreamSynchronize(algo->stream));
-            for (uint64_t i = 0; i < h.size(); i++) coords[i] = h[i];
         }
     });
 }

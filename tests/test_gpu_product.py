@@ -24,7 +24,7 @@ def run_product(dim, L, r, seed, **sched):
 @pytest.mark.parametrize("dim,L,r,phi_ref,tol", [
     (2, [1.0, 1.0], 0.005, 0.547187, 0.006),      # config 1 (reference: 6,967 discs, 0.547187)
     (3, [1.0, 1.0, 1.0], 0.02, 0.385201, 0.008),  # reference: 11,495 spheres, 0.38520
-    (2, [1.3, 0.7], 0.02, 0.500142 / (1.3 * 0.7) * (1.3 * 0.7), 0.03),
+    (2, [1.3, 0.7], 0.02, 0.500142 / (1.3 * 0.7), 0.03),  # reference n2d_rect_s7: 398 discs
 ])
 def test_product_run_is_valid_maximal_and_matches_fraction(dim, L, r, phi_ref, tol):
     dom, algo = run_product(dim, L, r, 7)
@@ -70,7 +70,7 @@ def test_dart_kernel_follows_pick_points_formula():
         assert key[i] == (int(w[8]) << 32) | i
 
 
-def _fresh(dim=2, L=(1.0, 1.0), r=0.05):
+def _fresh(dim=2, L=(1.0, 1.0), r=0.0625):
     rg = RadiusGenerator(dim, [(r, 10**9, 0)])
     dom = Domain([0.0] * dim, list(L), r)
     algo = Algo(dom, rg, 6000)
@@ -79,30 +79,42 @@ def _fresh(dim=2, L=(1.0, 1.0), r=0.05):
 
 
 def test_replay_edge_cases():
+    """Dyadic coordinates, so that every distance below is exact in FP64."""
     dom, algo = _fresh()
-    r = 0.05
+    r = 0.0625
+    k = lambda *v: np.array(v, np.uint64) << np.uint64(32)
     # empty round
     acc, n = algo.replay_round(np.zeros((0, 2)), np.zeros(0, np.uint64), np.zeros(0))
     assert n == 0 and len(acc) == 0
     # exact contact is not an overlap (dist^2 == (r1+r2)^2): both accepted
-    pos = np.array([[0.25, 0.5], [0.35, 0.5]])
-    acc, n = algo.replay_round(pos, np.array([1, 2], np.uint64) << np.uint64(32), np.full(2, r))
-    assert list(acc) == [True, True]
-    # equal priorities do not block each other (the reference's detection sees strictly smaller ones)
-    pos = np.array([[0.7, 0.2], [0.72, 0.2]])
-    acc, n = algo.replay_round(pos, np.array([5, 5], np.uint64) << np.uint64(32), np.full(2, r))
-    assert list(acc) == [True, True]
+    acc, n = algo.replay_round(np.array([[0.25, 0.5], [0.375, 0.5]]), k(1, 2), np.full(2, r))
+    assert list(acc) == [True, True] and n == 2
+    # one ulp closer than contact: overlap, the larger priority is rejected
+    acc, n = algo.replay_round(np.array([[0.25, 0.75], [np.nextafter(0.375, 0.0), 0.75]]), k(1, 2), np.full(2, r))
+    assert list(acc) == [True, False]
+    # equal priorities: the candidate index breaks the tie (the reference would accept both, overlapping)
+    acc, n = algo.replay_round(np.array([[0.75, 0.25], [0.8125, 0.25]]), k(5, 5), np.full(2, r))
+    assert list(acc) == [True, False]
+    acc, n = algo.replay_round(np.array([[0.8125, 0.0625], [0.75, 0.0625]]), k(5, 5), np.full(2, r))
+    assert list(acc) == [True, False]
     # a chain a < b < c with a-b and b-c overlapping: a and c accepted, b rejected
-    pos = np.array([[0.5, 0.85], [0.58, 0.85], [0.66, 0.85]])
-    acc, n = algo.replay_round(pos, np.array([1, 2, 3], np.uint64) << np.uint64(32), np.full(3, r))
+    acc, n = algo.replay_round(np.array([[0.5, 0.96875], [0.59375, 0.96875], [0.6875, 0.96875]]), k(1, 2, 3),
+                               np.full(3, r))
     assert list(acc) == [True, False, True]
-    # periodic wrap: a candidate near x = 1 overlaps a sphere near x = 0
-    pos = np.array([[0.02, 0.05]])
-    acc, _ = algo.replay_round(pos, np.array([1], np.uint64), np.full(1, r))
+    assert dom.check() == (0, 0)
+
+
+def test_replay_periodic_wrap():
+    dom, algo = _fresh()
+    r = 0.0625
+    acc, _ = algo.replay_round(np.array([[0.03125, 0.0625]]), np.array([1], np.uint64), np.full(1, r))
     assert list(acc) == [True]
-    pos = np.array([[0.95, 0.05], [0.99, 0.99]])
-    acc, _ = algo.replay_round(pos, np.array([1, 2], np.uint64), np.full(2, r))
-    assert list(acc) == [False, False]
+    # images x + L: across x = 1, across the corner, and exact contact through the boundary
+    pos = np.array([[0.9375, 0.0625], [0.96875, 0.96875], [0.90625, 0.5]])
+    acc, _ = algo.replay_round(pos, np.array([1, 2, 3], np.uint64), np.full(3, r))
+    assert list(acc) == [False, False, True]
+    acc, _ = algo.replay_round(np.array([[0.90625, 0.0625]]), np.array([1], np.uint64), np.full(1, r))
+    assert list(acc) == [True]  # 0.90625 + 0.125 = 1.03125 = 0.03125 + 1: exact contact
     assert dom.check() == (0, 0)
 
 
