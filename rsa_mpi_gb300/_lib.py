@@ -96,6 +96,8 @@ _SIGS = {
     "rsagpu_algo_draw_darts": (C.c_int, [_vp, C.c_uint64, C.c_uint64, C.c_uint64, _d, _u64, _u64]),
     "rsagpu_batch_run": (C.c_int, [C.POINTER(InstanceDesc), C.c_int, _u64, _d, _d]),
     "rsagpu_mlp_forward": (C.c_int, [_u16, _f32, C.c_uint64, _f32]),
+    "rsagpu_resolve_batch_noalloc": (C.c_int, [C.c_int, _d, _d, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_uint64, C.c_void_p, C.c_void_p]),
     "rsagpu_mlp_train_step": (C.c_int, [_f32, _u16, _f32, _f32, C.c_uint64, C.c_float, _f32, _f32]),
 }
 

@@ -96,6 +96,8 @@ void launch_scan_blocks(const uint32_t* counts, uint64_t* offsets, uint64_t n, u
 void launch_occ_block_counts(const uint32_t* occ, int64_t nwords, uint32_t* counts, cudaStream_t s);
 uint64_t kernel_launch_count();
 void count_launch(int n = 1);
+// text returned by rsagpu_last_error() for the calling thread
+void set_last_error(const char* msg);
 
 constexpr int REFINE_BLOCK = 256;
 constexpr int OCC_BLOCK = 256;  // words per extract block

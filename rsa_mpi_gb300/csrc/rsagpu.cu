@@ -777,6 +777,10 @@ rsagpu_radgen* make_radgen(int dim, const double* r, const uint64_t* n, const in
 
 }  // namespace
 
+namespace rsagpu {
+void set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+}  // namespace rsagpu
+
 // ================================================================================================
 // C ABI
 // ================================================================================================
