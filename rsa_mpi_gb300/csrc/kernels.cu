@@ -19,7 +19,7 @@ namespace {
 constexpr int D = RSA_DIM;
 constexpr int CHILDREN = 1 << D;
 constexpr int MASK_WORDS = (CHILDREN + 31) / 32;
-constexpr int K_PRE = 16;  // prefilter spheres kept in registers per parent voxel
+constexpr int K_PRE = 12;  // prefilter spheres kept per parent voxel (more: re-read from the grid)
 
 // Child order of subdivide_uncovered: TabCorner (auxiliary/Path.ixx:86-103) for D = 2, 3; for D >= 4
 // bit d of the child index is the offset along dimension d (the reference's generic table,
@@ -50,6 +50,8 @@ __host__ __device__ inline Grid<D> make_grid(const GridArgs& a) {
     g.phase = a.phase;
     g.stencil = a.stencil;
     g.S = a.S;
+    g.rows = a.rows;
+    g.R = a.R;
     return g;
 }
 
@@ -169,17 +171,18 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
 template <class F>
 __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c,
                                                  const int32_t* k, F&& f) {
-    for (int s = 0; s < g.S; s++) {
-        int8_t q[D];
-        const int64_t idx = stencil_cell<D>(g, k, s, q);
-        for (int32_t j = c.head[idx]; j >= 0; j = c.next[j]) {
-            double p[D], img[D];
+    walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q) {
+        for (int32_t x = lo; x <= hi; x++) {
+            for (int32_t j = c.head[base + x]; j >= 0; j = c.next[j]) {
+                double p[D], img[D];
 #pragma unroll
-            for (int d = 0; d < D; d++) p[d] = c.pos[(uint64_t)j * D + d];
-            image_of<D>(geo, p, q, img);
-            if (f(j, img)) return;
+                for (int d = 0; d < D; d++) p[d] = c.pos[(uint64_t)j * D + d];
+                image_of<D>(geo, p, q, img);
+                if (f(j, img)) return true;
+            }
         }
-    }
+        return false;
+    });
 }
 
 // candidate order: priority key, then candidate index (a strict total order; the reference's
@@ -235,8 +238,12 @@ __global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
 
 __global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
     if (c.und[it - 1] == 0) return;
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nalive = c.counters[0];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t rounds = (nalive + stride - 1) / stride;  // same trip count for every lane
+    for (uint32_t rr = 0; rr < rounds; rr++) {
+    const uint32_t t = t0 + rr * stride;
     bool still = false;
     if (t < nalive) {
         const uint32_t i = c.alive[t];
@@ -273,6 +280,7 @@ __global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
     }
     const uint32_t mask = __ballot_sync(0xffffffffu, still);
     if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[it], (uint32_t)__popc(mask));
+    }
 }
 
 // keys of the accepted candidates, for the count cap (retain_only_first_elements)
@@ -342,12 +350,71 @@ struct RefineParams {
     double inf[D];
     double rmin;
     uint32_t* masks;
+    uint32_t* warp_counts;
+    const uint64_t* warp_offsets;
+    uint32_t* err;
     uint32_t* survivors;
     unsigned long long* visits;
-    uint32_t* block_counts;
-    const uint64_t* block_offsets;
-    uint32_t* err;
 };
+
+// child index with bit d = offset along dimension d, for the child at position t of the corner table
+__device__ __forceinline__ int child_bits(int t) {
+    int j = 0;
+#pragma unroll
+    for (int d = 0; d < D; d++) j |= corner_bit(t, d) << d;
+    return j;
+}
+
+// Squared corner terms of one sphere for the two child origins along each dimension: origin t = 0 is the
+// parent's origin (2c nlen = c len exactly) and origin t = 1 is the parent's centre ((2c+1) nlen =
+// (c + 0.5) len exactly), so delta_t = img - origin_t are the parent's own differences.  sq[d][t] =
+// max over the child's two corners along d of the rounded square, and the child's rounded corner sum is
+// accumulated over d in order, as the reference's corner loop does.
+__device__ __forceinline__ uint32_t children_covered(const double* dl0, const double* dl1, const double* nlen,
+                                                     uint64_t R2b) {
+    constexpr int NC = CHILDREN <= 32 ? CHILDREN : 32;  // the wide variant serves D >= 6
+    constexpr int DD = CHILDREN <= 32 ? D : 5;
+    double acc[NC];
+    {
+        const double a0 = maxabs(dl0[0], __dsub_rn(nlen[0], dl0[0]));
+        const double a1 = maxabs(dl1[0], __dsub_rn(nlen[0], dl1[0]));
+        acc[0] = __dmul_rn(a0, a0);
+        acc[1] = __dmul_rn(a1, a1);
+    }
+#pragma unroll
+    for (int d = 1; d < DD; d++) {
+        const double a0 = maxabs(dl0[d], __dsub_rn(nlen[d], dl0[d]));
+        const double a1 = maxabs(dl1[d], __dsub_rn(nlen[d], dl1[d]));
+        const double s0 = __dmul_rn(a0, a0), s1 = __dmul_rn(a1, a1);
+#pragma unroll
+        for (int j = (1 << d) - 1; j >= 0; j--) {
+            acc[j | (1 << d)] = __dadd_rn(acc[j], s1);
+            acc[j] = __dadd_rn(acc[j], s0);
+        }
+    }
+    uint32_t cov = 0;  // bit t (corner-table order) set when the child is covered
+#pragma unroll
+    for (int t = 0; t < NC; t++) cov |= (dbits(acc[child_bits(t)]) <= R2b ? 1u : 0u) << t;
+    return cov;
+}
+
+__device__ __forceinline__ void children_covered_wide(const double* dl0, const double* dl1, const double* nlen,
+                                                      uint64_t R2b, uint32_t* cov) {
+    // D >= 6: 2^D children, same arithmetic as children_covered, one child at a time
+    for (int t = 0; t < CHILDREN; t++) {
+        const int j = child_bits(t);
+        double acc = 0.0;
+        for (int d = 0; d < D; d++) {
+            const double* dl = ((j >> d) & 1) ? dl1 : dl0;
+            const double a = maxabs(dl[d], __dsub_rn(nlen[d], dl[d]));
+            const double sq = __dmul_rn(a, a);
+            acc = d == 0 ? sq : __dadd_rn(acc, sq);
+        }
+        if (dbits(acc) <= R2b) cov[t >> 5] |= 1u << (t & 31);
+    }
+}
+
+constexpr uint64_t FAR_MARGIN_ULPS = 1ull << 13;  // relative 2^-39, far above the rounding of a distance
 
 __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> geo, RefineParams p) {
     const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
@@ -368,20 +435,44 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
         }
         int32_t k[D];
         cell_of<D>(g, geo, centre, k);
-        double pre[K_PRE][D];
-        double preR2[K_PRE];
+        double pre0[K_PRE][D], pre1[K_PRE][D];
+        uint64_t preR2[K_PRE];
         int npre = 0;
         bool overflow = false;
         const bool covered = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
             visits++;
             const double R = __dadd_rn(rs, p.rmin);
-            const double R2 = __dmul_rn(R, R);
-            if (!(maxcorner_dist2<D>(img, orig, p.len) > R2)) return true;  // parent fully covered
-            if (dist2_64<D>(img, centre) < R2) {
+            const uint64_t R2b = dbits(__dmul_rn(R, R));
+            // distance to the parent's centre: the prefilter of get_list_of_spheres (:283-307)
+            double dl1[D], s = 0.0;
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                dl1[d] = __dsub_rn(img[d], centre[d]);
+                const double sq = __dmul_rn(dl1[d], dl1[d]);
+                s = d == 0 ? sq : __dadd_rn(s, sq);
+            }
+            const uint64_t sb = dbits(s);
+            // A sphere that holds every corner holds the centre too: past R^2 (1 + 2^-39) it can neither
+            // cover the parent nor enter the prefilter list.
+            if (sb > R2b + FAR_MARGIN_ULPS) return false;
+            // is_in_sphere over the parent's corners (remove_covered, :30-54)
+            double dl0[D], m = 0.0;
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                dl0[d] = __dsub_rn(img[d], orig[d]);
+                const double a = maxabs(dl0[d], __dsub_rn(p.len[d], dl0[d]));
+                const double sq = __dmul_rn(a, a);
+                m = d == 0 ? sq : __dadd_rn(m, sq);
+            }
+            if (dbits(m) <= R2b) return true;  // the parent is covered
+            if (sb < R2b) {
                 if (npre < K_PRE) {
 #pragma unroll
-                    for (int d = 0; d < D; d++) pre[npre][d] = img[d];
-                    preR2[npre] = R2;
+                    for (int d = 0; d < D; d++) {
+                        pre0[npre][d] = dl0[d];
+                        pre1[npre][d] = dl1[d];
+                    }
+                    preR2[npre] = R2b;
                     npre++;
                 } else {
                     overflow = true;
@@ -389,42 +480,63 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
             }
             return false;
         });
-        survived = !covered;
         if (!covered) {
-            if (overflow) atomicOr(p.err, (uint32_t)ERR_PREFILTER_OVERFLOW);
-            for (int t = 0; t < CHILDREN; t++) {
-                double corig[D];
+            survived = true;
+            uint32_t cov[MASK_WORDS];
 #pragma unroll
-                for (int d = 0; d < D; d++)
-                    corig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)(2 * cc[d] + corner_bit(t, d)), p.nlen[d]));
-                bool ccov = false;
-                for (int s = 0; s < npre && !ccov; s++) ccov = !(maxcorner_dist2<D>(pre[s], corig, p.nlen) > preR2[s]);
-                if (!ccov && overflow) {
-                    ccov = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
-                        const double R = __dadd_rn(rs, p.rmin);
-                        const double R2 = __dmul_rn(R, R);
-                        if (!(dist2_64<D>(img, centre) < R2)) return false;
-                        return !(maxcorner_dist2<D>(img, corig, p.nlen) > R2);
-                    });
-                }
-                if (!ccov) mask[t >> 5] |= 1u << (t & 31);
+            for (int w = 0; w < MASK_WORDS; w++) cov[w] = 0;
+            for (int s = 0; s < npre; s++) {
+                if constexpr (CHILDREN <= 32) cov[0] |= children_covered(pre0[s], pre1[s], p.nlen, preR2[s]);
+                else children_covered_wide(pre0[s], pre1[s], p.nlen, preR2[s], cov);
+            }
+            if (overflow) {
+                atomicOr(p.err, (uint32_t)ERR_PREFILTER_OVERFLOW);
+                // the list was full: test every prefilter sphere again, straight from the grid
+                cov[0] = 0;
+                for (int w = 1; w < MASK_WORDS; w++) cov[w] = 0;
+                visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
+                    const double R = __dadd_rn(rs, p.rmin);
+                    const uint64_t R2b = dbits(__dmul_rn(R, R));
+                    double dl0[D], dl1[D], s = 0.0;
+#pragma unroll
+                    for (int d = 0; d < D; d++) {
+                        dl1[d] = __dsub_rn(img[d], centre[d]);
+                        const double sq = __dmul_rn(dl1[d], dl1[d]);
+                        s = d == 0 ? sq : __dadd_rn(s, sq);
+                        dl0[d] = __dsub_rn(img[d], orig[d]);
+                    }
+                    if (!(dbits(s) < R2b)) return false;
+                    if constexpr (CHILDREN <= 32) cov[0] |= children_covered(dl0, dl1, p.nlen, R2b);
+                    else children_covered_wide(dl0, dl1, p.nlen, R2b, cov);
+                    return false;
+                });
+            }
+#pragma unroll
+            for (int w = 0; w < MASK_WORDS; w++) {
+                const int bits_here = CHILDREN - 32 * w < 32 ? CHILDREN - 32 * w : 32;
+                const uint32_t all = bits_here >= 32 ? 0xffffffffu : ((1u << bits_here) - 1u);
+                mask[w] = ~cov[w] & all;
             }
         }
 #pragma unroll
         for (int w = 0; w < MASK_WORDS; w++) p.masks[v * MASK_WORDS + w] = mask[w];
     }
+    // per-warp child counts (no block barrier: warps that finish early leave)
     uint32_t cnt = 0;
 #pragma unroll
     for (int w = 0; w < MASK_WORDS; w++) cnt += __popc(mask[w]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     const uint32_t alive = __ballot_sync(0xffffffffu, survived);
-    if ((threadIdx.x & 31) == 0 && alive) atomicAdd(p.survivors, (uint32_t)__popc(alive));
     uint32_t wv = visits;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) wv += __shfl_xor_sync(0xffffffffu, wv, o);
-    if ((threadIdx.x & 31) == 0 && wv) atomicAdd(p.visits, (unsigned long long)wv);
-    uint32_t total;
-    block_exclusive_scan<REFINE_BLOCK>(cnt, &total);
-    if (threadIdx.x == 0) p.block_counts[blockIdx.x] = total;
+    if ((threadIdx.x & 31) == 0) {
+        const uint64_t warp = v >> 5;
+        if (warp * 32 < p.V) p.warp_counts[warp] = cnt;
+        if (alive) atomicAdd(p.survivors, (uint32_t)__popc(alive));
+        if (wv) atomicAdd(p.visits, (unsigned long long)wv);
+    }
 }
 
 __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
@@ -436,9 +548,15 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
         mask[w] = v < p.V ? p.masks[v * MASK_WORDS + w] : 0u;
         cnt += __popc(mask[w]);
     }
-    const uint32_t local = block_exclusive_scan<REFINE_BLOCK>(cnt, nullptr);
+    const int lane = threadIdx.x & 31;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
     if (v >= p.V || cnt == 0) return;
-    uint64_t o = p.block_offsets[blockIdx.x] + local;
+    uint64_t o = p.warp_offsets[v >> 5] + (incl - cnt);
     int64_t cc[D];
 #pragma unroll
     for (int d = 0; d < D; d++) cc[d] = p.vin[v * D + d];
@@ -578,7 +696,9 @@ void op_collect(const GridArgs& ga, const CandArgs& c, cudaStream_t s) {
 
 void op_settle(const GridArgs& ga, const CandArgs& c, int it, cudaStream_t s) {
     if (c.n == 0) return;
-    k_settle<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c, it);
+    // grid-stride over the alive list (its length is on the device): 8 blocks per SM at most
+    const unsigned nb = nblocks(c.n, 256) < 152u * 8u ? nblocks(c.n, 256) : 152u * 8u;
+    k_settle<<<nb, 256, 0, s>>>(make_grid(ga), make_geo(ga), c, it);
     count_launch();
 }
 
@@ -612,8 +732,8 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
     }
     p.rmin = a.rmin;
     p.masks = a.masks;
-    p.block_counts = a.block_counts;
-    p.block_offsets = a.block_offsets;
+    p.warp_counts = a.warp_counts;
+    p.warp_offsets = a.warp_offsets;
     p.err = a.err;
     p.survivors = a.survivors;
     p.visits = a.visits;

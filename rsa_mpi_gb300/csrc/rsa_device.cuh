@@ -28,7 +28,7 @@ enum : uint32_t {
     ERR_PREFILTER_OVERFLOW = 4u, // (informational) a parent voxel had more than K prefilter spheres
 };
 
-constexpr int NB = 8;      // stored lower-priority colliders per candidate
+constexpr int NB = 24;     // stored lower-priority colliders per candidate (more: rescan)
 constexpr int NB_OVERFLOW = 255;
 
 template <int D>
@@ -48,6 +48,9 @@ struct Grid {
     int32_t* phase;
     const int8_t* stencil;  // S offsets of D int8
     int S;
+    // the same stencil as rows along dimension 0: row r = {xlo, xhi, o_1, ..., o_{D-1}} (D+1 int8)
+    const int8_t* rows;
+    int R;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -155,20 +158,81 @@ __device__ __forceinline__ bool occupied(const uint32_t* occ, int64_t idx) {
     return (__ldg(occ + (idx >> 5)) >> (idx & 31)) & 1u;
 }
 
+// len (<= 32) occupancy bits of consecutive cells starting at linear index lin; the bitmap carries one
+// padding word so that the two-word window never reads past it.
+__device__ __forceinline__ uint32_t occ_bits(const uint32_t* occ, int64_t lin, int len) {
+    const int64_t w = lin >> 5;
+    const int sh = (int)(lin & 31);
+    const uint64_t win = ((uint64_t)__ldg(occ + w + 1) << 32) | (uint64_t)__ldg(occ + w);
+    const uint32_t bits = (uint32_t)(win >> sh);
+    return len >= 32 ? bits : (bits & ((1u << len) - 1u));
+}
+
+// Walks the stencil row by row: for each row, the wrapped cell coordinates of dimensions 1..D-1 and up to
+// three contiguous segments along dimension 0 (left wrap, inside, right wrap).  g(base + x, q) is called
+// per segment [lo, hi] with the image shifts q; it returns true to stop.
+template <int D, class G>
+__device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, int R, const int32_t* k, G&& g) {
+    for (int r = 0; r < R; r++) {
+        const int8_t* row = rows + r * (D + 1);
+        int8_t q[D];
+        int64_t base = 0;
+#pragma unroll
+        for (int d = D - 1; d >= 1; d--) {
+            int32_t kk = k[d] + (int32_t)row[1 + d];
+            int8_t qq = 0;
+            if (kk < 0) { kk += n[d]; qq = -1; }
+            else if (kk >= n[d]) { kk -= n[d]; qq = 1; }
+            q[d] = qq;
+            base = base * n[d] + kk;
+        }
+        base *= n[0];
+        const int32_t a = k[0] + (int32_t)row[0], b = k[0] + (int32_t)row[1];
+        if (a < 0) {
+            q[0] = -1;
+            if (g(base, a + n[0], (b < 0 ? b : -1) + n[0], q)) return true;
+        }
+        {
+            const int32_t lo = a > 0 ? a : 0, hi = b < n[0] - 1 ? b : n[0] - 1;
+            q[0] = 0;
+            if (lo <= hi && g(base, lo, hi, q)) return true;
+        }
+        if (b >= n[0]) {
+            q[0] = 1;
+            if (g(base, (a > n[0] ? a : n[0]) - n[0], b - n[0], q)) return true;
+        }
+    }
+    return false;
+}
+
 // Visits the placed spheres in the stencil around cell k; f(idx, img, r) returns true to stop.
 template <int D, class F>
 __device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo, const int32_t* k, F&& f) {
-    for (int s = 0; s < g.S; s++) {
-        int8_t q[D];
-        const int64_t idx = stencil_cell<D>(g, k, s, q);
-        if (!occupied(g.occ, idx)) continue;
-        double p[D], img[D];
+    return walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q) {
+        for (int32_t x = lo; x <= hi; x += 32) {
+            const int len = hi - x + 1 < 32 ? hi - x + 1 : 32;
+            uint32_t bits = occ_bits(g.occ, base + x, len);
+            while (bits) {
+                const int j = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const int64_t idx = base + x + j;
+                double p[D], img[D];
 #pragma unroll
-        for (int d = 0; d < D; d++) p[d] = g.pos[idx * D + d];
-        image_of<D>(geo, p, q, img);
-        if (f(idx, img, g.rad[idx])) return true;
-    }
-    return false;
+                for (int d = 0; d < D; d++) p[d] = g.pos[idx * D + d];
+                image_of<D>(geo, p, q, img);
+                if (f(idx, img, g.rad[idx])) return true;
+            }
+        }
+        return false;
+    });
+}
+
+// Bit patterns of non-negative doubles order like the values: integer max / compare on the ALU
+// instead of the FP64 pipe.
+__device__ __forceinline__ uint64_t dbits(double x) { return (uint64_t)__double_as_longlong(x); }
+__device__ __forceinline__ double maxabs(double a, double b) {
+    const uint64_t ua = dbits(a) & 0x7fffffffffffffffull, ub = dbits(b) & 0x7fffffffffffffffull;
+    return __longlong_as_double((long long)(ua > ub ? ua : ub));
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -22,6 +22,8 @@ struct GridArgs {
     int32_t* phase;
     const int8_t* stencil;
     int S;
+    const int8_t* rows;  // stencil rows along dimension 0: {xlo, xhi, o_1, ..., o_{D-1}}
+    int R;
 };
 
 struct CandArgs {
@@ -62,8 +64,8 @@ struct RefineArgs {
     double nlen[MAX_D];  // child length = 0.5 * parent
     double rmin;
     uint32_t* masks;     // W words per parent
-    uint32_t* block_counts;
-    uint64_t* block_offsets;
+    uint32_t* warp_counts;     // children kept per warp of 32 parents
+    uint64_t* warp_offsets;    // exclusive scan of warp_counts
     uint32_t* err;
     uint32_t* survivors;  // parents not covered (remove_covered keeps them)
     unsigned long long* visits;  // occupied stencil cells visited by the mask pass

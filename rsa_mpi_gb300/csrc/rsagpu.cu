@@ -148,9 +148,12 @@ struct SphereGrid {
     double rmin = 0, rmax = 0;
     GridArgs a{};
     std::vector<int8_t> stencil;
+    std::vector<int8_t> rows;
     int8_t* d_stencil = nullptr;
+    int8_t* d_rows = nullptr;
     int32_t* head = nullptr;
     void release() {
+        dfree(d_rows);
         dfree(a.occ);
         dfree(a.pos);
         dfree(a.rad);
@@ -322,7 +325,38 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
     G.d_stencil = dalloc<int8_t>(G.stencil.size());
     CK(cudaMemcpy(G.d_stencil, G.stencil.data(), G.stencil.size(), cudaMemcpyHostToDevice));
     a.stencil = G.d_stencil;
-    const int64_t nwords = (ncells + 31) / 32;
+    // the same offsets as rows along dimension 0: for each (o_1..o_{D-1}) the contiguous range of o_0
+    // (the bound is monotone in |o_0|), rows ordered by their nearest distance
+    {
+        std::vector<std::vector<int8_t>> rows;  // {xlo, xhi, o_1..o_{D-1}}
+        for (auto& v : offs) {
+            bool found = false;
+            for (auto& r : rows) {
+                bool same = true;
+                for (int d = 1; d < D; d++) same &= (r[1 + d] == v[d]);
+                if (same) {
+                    r[0] = std::min<int8_t>(r[0], v[0]);
+                    r[1] = std::max<int8_t>(r[1], v[0]);
+                    found = true;
+                    break;
+                }
+            }
+            if (!found) {
+                std::vector<int8_t> r(D + 1);
+                r[0] = r[1] = v[0];
+                for (int d = 1; d < D; d++) r[1 + d] = v[d];
+                rows.push_back(r);
+            }
+        }
+        G.rows.clear();
+        for (auto& r : rows) G.rows.insert(G.rows.end(), r.begin(), r.end());
+        a.R = (int)rows.size();
+        G.d_rows = dalloc<int8_t>(G.rows.size());
+        CK(cudaMemcpy(G.d_rows, G.rows.data(), G.rows.size(), cudaMemcpyHostToDevice));
+        a.rows = G.d_rows;
+    }
+    // one padding word: the two-word window of occ_bits reads up to word nwords
+    const int64_t nwords = (ncells + 31) / 32 + 1;
     a.occ = dalloc<uint32_t>(nwords);
     a.pos = dalloc<double>((uint64_t)ncells * D);
     a.rad = dalloc<double>(ncells);
@@ -387,7 +421,7 @@ void ensure_refine_buffers(rsagpu_algo* A, uint64_t V) {
         A->masks_cap = std::max<uint64_t>(words, A->masks_cap + A->masks_cap / 2);
         A->masks = dalloc<uint32_t>(A->masks_cap);
     }
-    const uint64_t blocks = (V + REFINE_BLOCK - 1) / REFINE_BLOCK + 1;
+    const uint64_t blocks = (V + 31) / 32 + 1;  // warp counts of the refinement
     const uint64_t oblocks = ((uint64_t)((A->dom->grid.a.ncells + 31) / 32) + OCC_BLOCK - 1) / OCC_BLOCK + 1;
     const uint64_t need = std::max(blocks, oblocks);
     if (need > A->blocks_cap) {
@@ -441,14 +475,14 @@ void refine(rsagpu_algo* A) {
     }
     r.rmin = A->rg.rmin();
     r.masks = A->masks;
-    r.block_counts = A->block_counts;
-    r.block_offsets = A->block_offsets;
+    r.warp_counts = A->block_counts;
+    r.warp_offsets = A->block_offsets;
     r.err = A->d_err;
     r.survivors = A->d_err + 1;
     r.visits = A->d_visits;
     CK(cudaMemsetAsync(r.survivors, 0, sizeof(uint32_t), A->stream));
     CK(cudaMemsetAsync(r.visits, 0, sizeof(unsigned long long), A->stream));
-    const uint64_t nb = (A->V + REFINE_BLOCK - 1) / REFINE_BLOCK;
+    const uint64_t nb = (A->V + 31) / 32;  // warps
     CK(cudaEventRecord(A->ev[8], A->stream));
     A->ops->refine_mask(A->dom->grid.a, r, A->stream);
     CK(cudaEventRecord(A->ev[9], A->stream));
@@ -564,16 +598,25 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
     ops->probe(g, c, A->stream);
     ev_record(A, 3);
     ops->collect(g, c, A->stream);
+    ev_record(A, 10);
+    if (A->timing) {
+        CK(cudaEventSynchronize(A->ev[10]));
+        A->stats.ms_probe += ev_ms(A, 2, 3);
+        A->stats.ms_settle += ev_ms(A, 3, 10);  // collect
+    }
     int it = 1;
     const int batch = 4;
     while (true) {
+        ev_record(A, 10);
         for (int b = 0; b < batch; b++, it++) {
             if (it > MAX_SETTLE) raise(RSAGPU_ERR_NO_PROGRESS, "settle did not converge in %d iterations", MAX_SETTLE);
             ops->settle(g, c, it, A->stream);
         }
+        ev_record(A, 11);
         CK(cudaMemcpyAsync(A->h_counters + COUNTERS + it - 1, c.und + it - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                            A->stream));
         CK(cudaStreamSynchronize(A->stream));
+        if (A->timing) A->stats.ms_settle += ev_ms(A, 10, 11);
         if (A->h_counters[COUNTERS + it - 1] == 0) break;
     }
     // settle iterations actually needed: the first zero counter
@@ -621,11 +664,7 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
         raise(RSAGPU_ERR_INVARIANT, "two accepted centres in one grid cell");
     (void)keep_state;
     A->placed += A->h_counters[1];
-    if (A->timing) {
-        A->stats.ms_probe += ev_ms(A, 2, 3);
-        A->stats.ms_settle += ev_ms(A, 3, 4);
-        A->stats.ms_commit += ev_ms(A, 4, 5);
-    }
+    if (A->timing) A->stats.ms_commit += ev_ms(A, 4, 5);
     return A->h_counters[1];
 }
 
