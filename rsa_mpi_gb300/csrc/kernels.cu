@@ -52,6 +52,16 @@ __host__ __device__ inline Grid<D> make_grid(const GridArgs& a) {
     g.S = a.S;
     g.rows = a.rows;
     g.R = a.R;
+    g.off = a.off;
+    g.radf = a.radf;
+    for (int d = 0; d < D; d++) {
+        g.c[d] = a.c[d];
+        g.cf[d] = a.cf[d];
+    }
+    g.guard = a.guard;
+    g.mono = a.mono;
+    g.rmono = a.rmono;
+    g.rmonof = (float)a.rmono;
     return g;
 }
 
@@ -141,9 +151,11 @@ __global__ void k_darts(DartParams p) {
 // (remove_collisions_with_validated_spheres, operator_cells_and_data_storage.ixx:54-76); the
 // others are linked into the candidate cell lists and appended to the alive list.
 // ------------------------------------------------------------------------------------------------
+template <bool F32>
 __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool alive = false;
+    uint32_t rt = 0;
     if (i < c.n && c.state[i] == ST_UNDECIDED) {
         double x[D];
 #pragma unroll
@@ -151,9 +163,39 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
         const double r = c.rad[i];
         int32_t k[D];
         cell_of<D>(g, geo, x, k);
-        const bool hit = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
-            return collide64<D>(r, x, rs, img);
-        });
+        bool hit;
+        if constexpr (!F32) {
+            hit = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
+                return collide64<D>(r, x, rs, img);
+            });
+        } else {
+            // FP32 screen: certain outside the guard band, FP64 retest inside it
+            float offq[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                const double base = __dadd_rn(geo.inf[d], __dmul_rn((double)k[d], g.c[d]));
+                offq[d] = __double2float_rn(__dsub_rn(x[d], base));
+                c.off[(uint64_t)i * D + d] = offq[d];
+                c.kc[(uint64_t)i * D + d] = k[d];
+            }
+            const float rf = __double2float_rn(r);
+            hit = visit_placed_o<D>(g, k, [&](int64_t idx, const int32_t* o, const int8_t* q) {
+                const float rs = g.mono ? g.rmonof : g.radf[idx];
+                const float R = __fadd_rn(rf, rs);
+                const float R2 = __fmul_rn(R, R);
+                float dlt[D];
+                model_delta<D>(g.cf, o, g.off + idx * D, offq, dlt);
+                const float d2 = sumsq32<D>(dlt);
+                if (d2 < __fsub_rn(R2, g.guard)) return true;
+                if (d2 > __fadd_rn(R2, g.guard)) return false;
+                rt++;
+                double p[D], img[D];
+#pragma unroll
+                for (int d = 0; d < D; d++) p[d] = g.pos[idx * D + d];
+                image_of<D>(geo, p, q, img);
+                return collide64<D>(r, x, g.mono ? g.rmono : g.rad[idx], img);
+            });
+        }
         if (hit) {
             c.state[i] = ST_DEAD;
         } else {
@@ -165,13 +207,18 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
     }
     const uint32_t slot = warp_append(&c.counters[0], alive);
     if (alive) c.alive[slot] = i;
+    if (F32) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rt += __shfl_xor_sync(0xffffffffu, rt, o);
+        if ((threadIdx.x & 31) == 0 && rt) atomicAdd(&c.counters[4], rt);
+    }
 }
 
 // Visits the same-round candidates in the stencil around cell k (linked lists head/next).
 template <class F>
 __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c,
                                                  const int32_t* k, F&& f) {
-    walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q) {
+    walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
         for (int32_t x = lo; x <= hi; x++) {
             for (int32_t j = c.head[base + x]; j >= 0; j = c.next[j]) {
                 double p[D], img[D];
@@ -183,6 +230,43 @@ __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>&
         }
         return false;
     });
+}
+
+// Same walk with the integer cell offset o of each candidate (FP32 screen); f(j, o, q).
+template <class F>
+__device__ __forceinline__ void visit_candidates_o(const Grid<D>& g, const CandArgs& c, const int32_t* k, F&& f) {
+    walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
+        int32_t o[D];
+#pragma unroll
+        for (int d = 1; d < D; d++) o[d] = row[1 + d];
+        const int32_t shift0 = (q[0] < 0 ? -g.n[0] : (q[0] > 0 ? g.n[0] : 0)) - k[0];
+        for (int32_t x = lo; x <= hi; x++) {
+            o[0] = x + shift0;
+            for (int32_t j = c.head[base + x]; j >= 0; j = c.next[j])
+                if (f(j, o, q)) return true;
+        }
+        return false;
+    });
+}
+
+// Screened overlap test of candidate i (FP32 data offq, rf; FP64 data x, r) with candidate j seen at
+// cell offset o and image shift q: certain outside the guard band, FP64 retest inside it.
+__device__ __forceinline__ bool cand_collide32(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, const double* x,
+                                               double r, const float* offq, float rf, int32_t j, const int32_t* o,
+                                               const int8_t* q, uint32_t& rt) {
+    const float R = __fadd_rn(rf, __double2float_rn(c.rad[j]));
+    const float R2 = __fmul_rn(R, R);
+    float dlt[D];
+    model_delta<D>(g.cf, o, c.off + (uint64_t)j * D, offq, dlt);
+    const float d2 = sumsq32<D>(dlt);
+    if (d2 < __fsub_rn(R2, g.guard)) return true;
+    if (d2 > __fadd_rn(R2, g.guard)) return false;
+    rt++;
+    double p[D], img[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) p[d] = c.pos[(uint64_t)j * D + d];
+    image_of<D>(geo, p, q, img);
+    return collide64<D>(r, x, c.rad[j], img);
 }
 
 // candidate order: priority key, then candidate index (a strict total order; the reference's
@@ -204,10 +288,12 @@ __device__ __forceinline__ uint8_t load_state(const uint8_t* s, int32_t j) {
 // candidate whose blockers are all rejected and reject one with an accepted blocker.  The smallest
 // undecided key always settles, so each iteration makes progress.
 // ------------------------------------------------------------------------------------------------
+template <bool F32>
 __global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nalive = c.counters[0];
     bool undecided = false;
+    uint32_t rt = 0;
     if (t < nalive) {
         const uint32_t i = c.alive[t];
         double x[D];
@@ -215,16 +301,34 @@ __global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
         for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
         const double r = c.rad[i];
         const uint64_t key = c.key[i];
-        int32_t k[D];
-        cell_of<D>(g, geo, x, k);
         int nb = 0;
-        visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
-            if (!precedes(c.key[j], j, key, i)) return false;
-            if (!collide64<D>(r, x, c.rad[j], img)) return false;
+        auto record = [&](int32_t j) {
             if (nb < NB) c.blk[(uint64_t)i * NB + nb] = j;
             nb++;
-            return false;
-        });
+        };
+        if constexpr (!F32) {
+            int32_t k[D];
+            cell_of<D>(g, geo, x, k);
+            visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
+                if (!precedes(c.key[j], j, key, i)) return false;
+                if (collide64<D>(r, x, c.rad[j], img)) record(j);
+                return false;
+            });
+        } else {
+            int32_t k[D];
+            float offq[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                k[d] = c.kc[(uint64_t)i * D + d];
+                offq[d] = c.off[(uint64_t)i * D + d];
+            }
+            const float rf = __double2float_rn(r);
+            visit_candidates_o(g, c, k, [&](int32_t j, const int32_t* o, const int8_t* q) {
+                if (!precedes(c.key[j], j, key, i)) return false;
+                if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) record(j);
+                return false;
+            });
+        }
         if (nb == 0) {
             c.state[i] = ST_ACCEPTED;
         } else {
@@ -234,52 +338,78 @@ __global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
     }
     const uint32_t mask = __ballot_sync(0xffffffffu, undecided);
     if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[0], (uint32_t)__popc(mask));
+    if (F32) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rt += __shfl_xor_sync(0xffffffffu, rt, o);
+        if ((threadIdx.x & 31) == 0 && rt) atomicAdd(&c.counters[4], rt);
+    }
 }
 
+template <bool F32>
 __global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
     if (c.und[it - 1] == 0) return;
     const uint32_t nalive = c.counters[0];
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t rounds = (nalive + stride - 1) / stride;  // same trip count for every lane
+    uint32_t rt = 0;
     for (uint32_t rr = 0; rr < rounds; rr++) {
-    const uint32_t t = t0 + rr * stride;
-    bool still = false;
-    if (t < nalive) {
-        const uint32_t i = c.alive[t];
-        if (load_state(c.state, i) == ST_UNDECIDED) {
-            bool any_acc = false, all_rej = true;
-            const uint8_t nb = c.nblk[i];
-            if (nb != NB_OVERFLOW) {
-                for (int j = 0; j < nb; j++) {
-                    const uint8_t s = load_state(c.state, c.blk[(uint64_t)i * NB + j]);
-                    any_acc |= (s == ST_ACCEPTED);
-                    all_rej &= (s == ST_REJECTED);
-                }
-            } else {
-                double x[D];
-#pragma unroll
-                for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
-                const double r = c.rad[i];
-                const uint64_t key = c.key[i];
-                int32_t k[D];
-                cell_of<D>(g, geo, x, k);
-                visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
-                    if (!precedes(c.key[j], j, key, i)) return false;
-                    if (!collide64<D>(r, x, c.rad[j], img)) return false;
+        const uint32_t t = t0 + rr * stride;
+        bool still = false;
+        if (t < nalive) {
+            const uint32_t i = c.alive[t];
+            if (load_state(c.state, i) == ST_UNDECIDED) {
+                bool any_acc = false, all_rej = true;
+                const uint8_t nb = c.nblk[i];
+                auto judge = [&](int32_t j) {
                     const uint8_t s = load_state(c.state, j);
                     any_acc |= (s == ST_ACCEPTED);
                     all_rej &= (s == ST_REJECTED);
-                    return any_acc;
-                });
+                };
+                if (nb != NB_OVERFLOW) {
+                    for (int b = 0; b < nb; b++) judge(c.blk[(uint64_t)i * NB + b]);
+                } else {
+                    double x[D];
+#pragma unroll
+                    for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
+                    const double r = c.rad[i];
+                    const uint64_t key = c.key[i];
+                    if constexpr (!F32) {
+                        int32_t k[D];
+                        cell_of<D>(g, geo, x, k);
+                        visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
+                            if (!precedes(c.key[j], j, key, i)) return false;
+                            if (collide64<D>(r, x, c.rad[j], img)) judge(j);
+                            return any_acc;
+                        });
+                    } else {
+                        int32_t k[D];
+                        float offq[D];
+#pragma unroll
+                        for (int d = 0; d < D; d++) {
+                            k[d] = c.kc[(uint64_t)i * D + d];
+                            offq[d] = c.off[(uint64_t)i * D + d];
+                        }
+                        const float rf = __double2float_rn(r);
+                        visit_candidates_o(g, c, k, [&](int32_t j, const int32_t* o, const int8_t* q) {
+                            if (!precedes(c.key[j], j, key, i)) return false;
+                            if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) judge(j);
+                            return any_acc;
+                        });
+                    }
+                }
+                if (any_acc) c.state[i] = ST_REJECTED;
+                else if (all_rej) c.state[i] = ST_ACCEPTED;
+                else still = true;
             }
-            if (any_acc) c.state[i] = ST_REJECTED;
-            else if (all_rej) c.state[i] = ST_ACCEPTED;
-            else still = true;
         }
+        const uint32_t mask = __ballot_sync(0xffffffffu, still);
+        if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[it], (uint32_t)__popc(mask));
     }
-    const uint32_t mask = __ballot_sync(0xffffffffu, still);
-    if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[it], (uint32_t)__popc(mask));
+    if (F32) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rt += __shfl_xor_sync(0xffffffffu, rt, o);
+        if ((threadIdx.x & 31) == 0 && rt) atomicAdd(&c.counters[4], rt);
     }
 }
 
@@ -311,7 +441,7 @@ __global__ void k_cut_accepted(CandArgs c, int use_pivot, double pivot, uint64_t
 }
 
 // commit: accepted candidates become placed spheres; the candidate lists are cleared.
-__global__ void k_commit(Grid<D> g, CandArgs c) {
+__global__ void k_commit(Grid<D> g, Geo<D> geo, CandArgs c) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nalive = c.counters[0];
     bool acc = false;
@@ -324,9 +454,19 @@ __global__ void k_commit(Grid<D> g, CandArgs c) {
             const uint32_t bit = 1u << (idx & 31);
             const uint32_t old = atomicOr(g.occ + (idx >> 5), bit);
             if (old & bit) atomicOr(&c.counters[2], (uint32_t)ERR_DOUBLE_OCCUPANCY);
+            int64_t rem = idx;
 #pragma unroll
-            for (int d = 0; d < D; d++) g.pos[idx * D + d] = c.pos[(uint64_t)i * D + d];
+            for (int d = 0; d < D; d++) {
+                const int32_t kd = (int32_t)(rem % g.n[d]);
+                rem /= g.n[d];
+                const double x = c.pos[(uint64_t)i * D + d];
+                g.pos[idx * D + d] = x;
+                // FP32 screening offset from the cell's corner (guard-band form)
+                const double base = __dadd_rn(geo.inf[d], __dmul_rn((double)kd, g.c[d]));
+                ((float*)g.off)[idx * D + d] = __double2float_rn(__dsub_rn(x, base));
+            }
             g.rad[idx] = c.rad[i];
+            ((float*)g.radf)[idx] = __double2float_rn(c.rad[i]);
             g.phase[idx] = c.phase[i];
         }
     }
@@ -355,6 +495,10 @@ struct RefineParams {
     uint32_t* err;
     uint32_t* survivors;
     unsigned long long* visits;
+    unsigned long long* retests;
+    float lenf[D];
+    float nlenf[D];
+    float rminf;
 };
 
 // child index with bit d = offset along dimension d, for the child at position t of the corner table
@@ -539,6 +683,210 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
     }
 }
 
+// FP32 form of k_refine_mask: the same decisions, screened in FP32 against the guard band.  Per voxel the
+// origin, centre and their offsets from the centre's cell corner are computed in FP64 (O(D) work);
+// each (voxel, sphere) test is FP32 unless it falls inside the guard band, where it is redone in FP64
+// exactly as the FP64 kernel does.
+__global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask32(Grid<D> g, Geo<D> geo, RefineParams p) {
+    const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
+    uint32_t mask[MASK_WORDS];
+#pragma unroll
+    for (int w = 0; w < MASK_WORDS; w++) mask[w] = 0;
+    bool survived = false;
+    uint32_t visits = 0, rt = 0;
+    if (v < p.V) {
+        int64_t cc[D];
+        double orig[D], centre[D];
+        float relo[D], relc[D];
+        int32_t k[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            cc[d] = p.vin[v * D + d];
+            orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cc[d], p.len[d]));
+            centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cc[d], 0.5), p.len[d]));
+        }
+        cell_of<D>(g, geo, centre, k);
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const double base = __dadd_rn(geo.inf[d], __dmul_rn((double)k[d], g.c[d]));
+            relo[d] = __double2float_rn(__dsub_rn(orig[d], base));
+            relc[d] = __double2float_rn(__dsub_rn(centre[d], base));
+        }
+        float pre0[K_PRE][D], pre1[K_PRE][D], preR2[K_PRE];
+        int64_t preidx[K_PRE];
+        uint32_t preq[K_PRE];  // 2 bits per dimension: image shift + 1
+        int npre = 0;
+        bool overflow = false;
+        // exact FP64 differences of one (voxel, sphere) pair, for the guard band
+        auto exact_deltas = [&](int64_t idx, const int8_t* q, double* dl0, double* dl1) {
+            double pp[D], img[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) pp[d] = g.pos[idx * D + d];
+            image_of<D>(geo, pp, q, img);
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                dl0[d] = __dsub_rn(img[d], orig[d]);
+                dl1[d] = __dsub_rn(img[d], centre[d]);
+            }
+        };
+        auto exact_R2b = [&](int64_t idx) {
+            const double R = __dadd_rn(g.mono ? g.rmono : g.rad[idx], p.rmin);
+            return dbits(__dmul_rn(R, R));
+        };
+        const bool covered = visit_placed_o<D>(g, k, [&](int64_t idx, const int32_t* o, const int8_t* q) {
+            visits++;
+            const float rs = g.mono ? g.rmonof : g.radf[idx];
+            const float R = __fadd_rn(rs, p.rminf);
+            const float R2 = __fmul_rn(R, R);
+            const float lo = __fsub_rn(R2, g.guard), hi = __fadd_rn(R2, g.guard);
+            const float* offs = g.off + idx * D;
+            float d1[D];
+            model_delta<D>(g.cf, o, offs, relc, d1);
+            const float s1 = sumsq32<D>(d1);
+            if (s1 > hi) return false;  // far: covers nothing, not in the prefilter list
+            float d0[D];
+            model_delta<D>(g.cf, o, offs, relo, d0);
+            float m = 0.f;
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                const float a = fmaxf(fabsf(d0[d]), fabsf(__fsub_rn(p.lenf[d], d0[d])));
+                m = __fadd_rn(m, __fmul_rn(a, a));
+            }
+            if (m < lo) return true;  // the parent is covered
+            bool in_pre = s1 < lo;
+            if (m <= hi || (!in_pre && s1 <= hi)) {
+                // guard band: redo this pair in FP64, as the FP64 kernel does
+                rt++;
+                double dl0[D], dl1[D];
+                exact_deltas(idx, q, dl0, dl1);
+                const uint64_t R2b = exact_R2b(idx);
+                double mm = 0.0, ss = 0.0;
+#pragma unroll
+                for (int d = 0; d < D; d++) {
+                    const double a = maxabs(dl0[d], __dsub_rn(p.len[d], dl0[d]));
+                    const double sq = __dmul_rn(a, a);
+                    mm = d == 0 ? sq : __dadd_rn(mm, sq);
+                    const double s2 = __dmul_rn(dl1[d], dl1[d]);
+                    ss = d == 0 ? s2 : __dadd_rn(ss, s2);
+                }
+                if (dbits(mm) <= R2b) return true;
+                in_pre = dbits(ss) < R2b;
+            }
+            if (in_pre) {
+                if (npre < K_PRE) {
+#pragma unroll
+                    for (int d = 0; d < D; d++) {
+                        pre0[npre][d] = d0[d];
+                        pre1[npre][d] = d1[d];
+                    }
+                    preR2[npre] = R2;
+                    preidx[npre] = idx;
+                    uint32_t qq = 0;
+#pragma unroll
+                    for (int d = 0; d < D; d++) qq |= (uint32_t)(q[d] + 1) << (2 * d);
+                    preq[npre] = qq;
+                    npre++;
+                } else {
+                    overflow = true;
+                }
+            }
+            return false;
+        });
+        if (!covered) {
+            survived = true;
+            uint32_t cov[MASK_WORDS];
+#pragma unroll
+            for (int w = 0; w < MASK_WORDS; w++) cov[w] = 0;
+            for (int sidx = 0; sidx < npre; sidx++) {
+                // children of this sphere in FP32; any child inside the guard band -> this sphere in FP64
+                const float lo = __fsub_rn(preR2[sidx], g.guard), hi = __fadd_rn(preR2[sidx], g.guard);
+                bool band = false;
+                uint32_t c32[MASK_WORDS];
+#pragma unroll
+                for (int w = 0; w < MASK_WORDS; w++) c32[w] = 0;
+                for (int t = 0; t < CHILDREN; t++) {
+                    const int jb = child_bits(t);
+                    float acc = 0.f;
+#pragma unroll
+                    for (int d = 0; d < D; d++) {
+                        const float dd = ((jb >> d) & 1) ? pre1[sidx][d] : pre0[sidx][d];
+                        const float a = fmaxf(fabsf(dd), fabsf(__fsub_rn(p.nlenf[d], dd)));
+                        acc = __fadd_rn(acc, __fmul_rn(a, a));
+                    }
+                    if (acc < lo) c32[t >> 5] |= 1u << (t & 31);
+                    else if (acc <= hi) band = true;
+                }
+                if (band) {
+                    rt++;
+                    int8_t q[D];
+#pragma unroll
+                    for (int d = 0; d < D; d++) q[d] = (int8_t)((preq[sidx] >> (2 * d)) & 3u) - 1;
+                    double dl0[D], dl1[D];
+                    exact_deltas(preidx[sidx], q, dl0, dl1);
+                    const uint64_t R2b = exact_R2b(preidx[sidx]);
+                    if constexpr (CHILDREN <= 32) c32[0] = children_covered(dl0, dl1, p.nlen, R2b);
+                    else {
+#pragma unroll
+                        for (int w = 0; w < MASK_WORDS; w++) c32[w] = 0;
+                        children_covered_wide(dl0, dl1, p.nlen, R2b, c32);
+                    }
+                }
+#pragma unroll
+                for (int w = 0; w < MASK_WORDS; w++) cov[w] |= c32[w];
+            }
+            if (overflow) {
+                atomicOr(p.err, (uint32_t)ERR_PREFILTER_OVERFLOW);
+                // the list was full: every prefilter sphere again, in FP64, straight from the grid
+#pragma unroll
+                for (int w = 0; w < MASK_WORDS; w++) cov[w] = 0;
+                visit_placed<D>(g, geo, k, [&](int64_t idx, const double* img, double rs) {
+                    const double R = __dadd_rn(rs, p.rmin);
+                    const uint64_t R2b = dbits(__dmul_rn(R, R));
+                    double dl0[D], dl1[D], ss = 0.0;
+#pragma unroll
+                    for (int d = 0; d < D; d++) {
+                        dl1[d] = __dsub_rn(img[d], centre[d]);
+                        const double sq = __dmul_rn(dl1[d], dl1[d]);
+                        ss = d == 0 ? sq : __dadd_rn(ss, sq);
+                        dl0[d] = __dsub_rn(img[d], orig[d]);
+                    }
+                    if (!(dbits(ss) < R2b)) return false;
+                    if constexpr (CHILDREN <= 32) cov[0] |= children_covered(dl0, dl1, p.nlen, R2b);
+                    else children_covered_wide(dl0, dl1, p.nlen, R2b, cov);
+                    return false;
+                });
+            }
+#pragma unroll
+            for (int w = 0; w < MASK_WORDS; w++) {
+                const int bits_here = CHILDREN - 32 * w < 32 ? CHILDREN - 32 * w : 32;
+                const uint32_t all = bits_here >= 32 ? 0xffffffffu : ((1u << bits_here) - 1u);
+                mask[w] = ~cov[w] & all;
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < MASK_WORDS; w++) p.masks[v * MASK_WORDS + w] = mask[w];
+    }
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int w = 0; w < MASK_WORDS; w++) cnt += __popc(mask[w]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    const uint32_t alive = __ballot_sync(0xffffffffu, survived);
+    uint32_t wv = visits, wr = rt;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        wv += __shfl_xor_sync(0xffffffffu, wv, o);
+        wr += __shfl_xor_sync(0xffffffffu, wr, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        const uint64_t warp = v >> 5;
+        if (warp * 32 < p.V) p.warp_counts[warp] = cnt;
+        if (alive) atomicAdd(p.survivors, (uint32_t)__popc(alive));
+        if (wv) atomicAdd(p.visits, (unsigned long long)wv);
+        if (wr) atomicAdd(p.retests, (unsigned long long)wr);
+    }
+}
+
 __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
     const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
     uint32_t mask[MASK_WORDS];
@@ -682,23 +1030,26 @@ void op_darts(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaStre
     count_launch();
 }
 
-void op_probe(const GridArgs& ga, const CandArgs& c, cudaStream_t s) {
+void op_probe(const GridArgs& ga, const CandArgs& c, int f32, cudaStream_t s) {
     if (c.n == 0) return;
-    k_probe<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    if (f32) k_probe<true><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    else k_probe<false><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
     count_launch();
 }
 
-void op_collect(const GridArgs& ga, const CandArgs& c, cudaStream_t s) {
+void op_collect(const GridArgs& ga, const CandArgs& c, int f32, cudaStream_t s) {
     if (c.n == 0) return;
-    k_collect<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    if (f32) k_collect<true><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    else k_collect<false><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
     count_launch();
 }
 
-void op_settle(const GridArgs& ga, const CandArgs& c, int it, cudaStream_t s) {
+void op_settle(const GridArgs& ga, const CandArgs& c, int it, int f32, cudaStream_t s) {
     if (c.n == 0) return;
     // grid-stride over the alive list (its length is on the device): 8 blocks per SM at most
     const unsigned nb = nblocks(c.n, 256) < 152u * 8u ? nblocks(c.n, 256) : 152u * 8u;
-    k_settle<<<nb, 256, 0, s>>>(make_grid(ga), make_geo(ga), c, it);
+    if (f32) k_settle<true><<<nb, 256, 0, s>>>(make_grid(ga), make_geo(ga), c, it);
+    else k_settle<false><<<nb, 256, 0, s>>>(make_grid(ga), make_geo(ga), c, it);
     count_launch();
 }
 
@@ -716,7 +1067,7 @@ void op_cut_accepted(const CandArgs& c, int use_pivot, double pivot, uint64_t ke
 
 void op_commit(const GridArgs& ga, const CandArgs& c, cudaStream_t s) {
     if (c.n == 0) return;
-    k_commit<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), c);
+    k_commit<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
     count_launch();
 }
 
@@ -737,12 +1088,21 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
     p.err = a.err;
     p.survivors = a.survivors;
     p.visits = a.visits;
+    p.retests = a.retests;
+    for (int d = 0; d < D; d++) {
+        p.lenf[d] = (float)a.len[d];
+        p.nlenf[d] = (float)a.nlen[d];
+    }
+    p.rminf = (float)a.rmin;
     return p;
 }
 
-void op_refine_mask(const GridArgs& ga, const RefineArgs& a, cudaStream_t s) {
+void op_refine_mask(const GridArgs& ga, const RefineArgs& a, int f32, cudaStream_t s) {
     if (a.V == 0) return;
-    k_refine_mask<<<nblocks(a.V, REFINE_BLOCK), REFINE_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
+    if (f32)
+        k_refine_mask32<<<nblocks(a.V, REFINE_BLOCK), REFINE_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
+    else
+        k_refine_mask<<<nblocks(a.V, REFINE_BLOCK), REFINE_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
     count_launch();
 }
 

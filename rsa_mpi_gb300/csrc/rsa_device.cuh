@@ -51,6 +51,16 @@ struct Grid {
     // the same stencil as rows along dimension 0: row r = {xlo, xhi, o_1, ..., o_{D-1}} (D+1 int8)
     const int8_t* rows;
     int R;
+    // FP32 screening representation of the placed centres (guard-band form): off = centre minus the
+    // corner of its cell, rounded to float; radf = radius rounded to float
+    const float* off;
+    const float* radf;
+    double c[D];    // cell edge
+    float cf[D];    // cell edge rounded to float
+    float guard;    // bound on |FP32 model - FP64 value| of any squared distance the kernels compare
+    int mono;       // one radius for every sphere
+    double rmono;
+    float rmonof;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -169,8 +179,8 @@ __device__ __forceinline__ uint32_t occ_bits(const uint32_t* occ, int64_t lin, i
 }
 
 // Walks the stencil row by row: for each row, the wrapped cell coordinates of dimensions 1..D-1 and up to
-// three contiguous segments along dimension 0 (left wrap, inside, right wrap).  g(base + x, q) is called
-// per segment [lo, hi] with the image shifts q; it returns true to stop.
+// three contiguous segments along dimension 0 (left wrap, inside, right wrap).  g(base, lo, hi, q, row) is
+// called per segment [lo, hi] with the image shifts q; it returns true to stop.
 template <int D, class G>
 __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, int R, const int32_t* k, G&& g) {
     for (int r = 0; r < R; r++) {
@@ -190,16 +200,16 @@ __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, 
         const int32_t a = k[0] + (int32_t)row[0], b = k[0] + (int32_t)row[1];
         if (a < 0) {
             q[0] = -1;
-            if (g(base, a + n[0], (b < 0 ? b : -1) + n[0], q)) return true;
+            if (g(base, a + n[0], (b < 0 ? b : -1) + n[0], q, row)) return true;
         }
         {
             const int32_t lo = a > 0 ? a : 0, hi = b < n[0] - 1 ? b : n[0] - 1;
             q[0] = 0;
-            if (lo <= hi && g(base, lo, hi, q)) return true;
+            if (lo <= hi && g(base, lo, hi, q, row)) return true;
         }
         if (b >= n[0]) {
             q[0] = 1;
-            if (g(base, (a > n[0] ? a : n[0]) - n[0], b - n[0], q)) return true;
+            if (g(base, (a > n[0] ? a : n[0]) - n[0], b - n[0], q, row)) return true;
         }
     }
     return false;
@@ -208,7 +218,7 @@ __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, 
 // Visits the placed spheres in the stencil around cell k; f(idx, img, r) returns true to stop.
 template <int D, class F>
 __device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo, const int32_t* k, F&& f) {
-    return walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q) {
+    return walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
         for (int32_t x = lo; x <= hi; x += 32) {
             const int len = hi - x + 1 < 32 ? hi - x + 1 : 32;
             uint32_t bits = occ_bits(g.occ, base + x, len);
@@ -225,6 +235,46 @@ __device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo
         }
         return false;
     });
+}
+
+// Visits the placed spheres in the stencil around cell k with their integer cell offset o (the periodic
+// shift folded in: o = cell of the image - k); f(idx, o, q) returns true to stop.
+template <int D, class F>
+__device__ __forceinline__ bool visit_placed_o(const Grid<D>& g, const int32_t* k, F&& f) {
+    return walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
+        int32_t o[D];
+#pragma unroll
+        for (int d = 1; d < D; d++) o[d] = row[1 + d];
+        const int32_t shift0 = (q[0] < 0 ? -g.n[0] : (q[0] > 0 ? g.n[0] : 0)) - k[0];
+        for (int32_t x = lo; x <= hi; x += 32) {
+            const int len = hi - x + 1 < 32 ? hi - x + 1 : 32;
+            uint32_t bits = occ_bits(g.occ, base + x, len);
+            while (bits) {
+                const int j = __ffs(bits) - 1;
+                bits &= bits - 1;
+                o[0] = x + j + shift0;
+                if (f(base + x + j, o, q)) return true;
+            }
+        }
+        return false;
+    });
+}
+
+// FP32 model of (image of a stored centre) - (query point): o c + (off_s - off_q), with o the integer
+// cell offset; its error against the FP64 difference is bounded by the guard band of the grid.
+template <int D>
+__device__ __forceinline__ void model_delta(const float* cf, const int32_t* o, const float* off_s, const float* off_q,
+                                            float* dlt) {
+#pragma unroll
+    for (int d = 0; d < D; d++) dlt[d] = __fadd_rn(__fmul_rn((float)o[d], cf[d]), __fsub_rn(off_s[d], off_q[d]));
+}
+
+template <int D>
+__device__ __forceinline__ float sumsq32(const float* v) {
+    float s = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; d++) s = __fadd_rn(s, __fmul_rn(v[d], v[d]));
+    return s;
 }
 
 // Bit patterns of non-negative doubles order like the values: integer max / compare on the ALU

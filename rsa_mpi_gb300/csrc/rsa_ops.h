@@ -24,6 +24,13 @@ struct GridArgs {
     int S;
     const int8_t* rows;  // stencil rows along dimension 0: {xlo, xhi, o_1, ..., o_{D-1}}
     int R;
+    float* off;          // FP32 screening offsets (D floats per cell)
+    float* radf;         // radii rounded to float
+    double c[MAX_D];     // cell edge
+    float cf[MAX_D];     // cell edge rounded to float
+    float guard;         // guard band of the FP32 screen (absolute, on squared distances)
+    int mono;            // one radius class
+    double rmono;
 };
 
 struct CandArgs {
@@ -37,7 +44,9 @@ struct CandArgs {
     int32_t* next;      // linked list of candidates per cell
     int32_t* head;      // per grid cell, -1 = no candidate
     uint32_t* alive;    // candidates that survived the probe
-    uint32_t* counters; // [0] = alive count, [1] = accepted count, [2] = error bits, [3] = gathered
+    uint32_t* counters; // [0] = alive, [1] = accepted, [2] = error bits, [3] = gathered, [4] = FP64 retests
+    float* off;         // FP32 screening offsets of the candidates (guard-band form)
+    int32_t* kc;        // cell coordinates of the candidates (guard-band form)
     int32_t* blk;       // NB lower-priority colliders per candidate
     uint8_t* nblk;
     uint32_t* und;      // undecided count after each settle iteration (und[0] after collect)
@@ -69,19 +78,20 @@ struct RefineArgs {
     uint32_t* err;
     uint32_t* survivors;  // parents not covered (remove_covered keeps them)
     unsigned long long* visits;  // occupied stencil cells visited by the mask pass
+    unsigned long long* retests; // (voxel, sphere) pairs redone in FP64 (guard-band form)
 };
 
 struct DimOps {
     int D;
     void (*vox_init)(int64_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s);
     void (*darts)(const GridArgs& g, const CandArgs& c, const DartArgs& a, cudaStream_t s);
-    void (*probe)(const GridArgs& g, const CandArgs& c, cudaStream_t s);
-    void (*collect)(const GridArgs& g, const CandArgs& c, cudaStream_t s);
-    void (*settle)(const GridArgs& g, const CandArgs& c, int iteration, cudaStream_t s);
+    void (*probe)(const GridArgs& g, const CandArgs& c, int f32, cudaStream_t s);
+    void (*collect)(const GridArgs& g, const CandArgs& c, int f32, cudaStream_t s);
+    void (*settle)(const GridArgs& g, const CandArgs& c, int iteration, int f32, cudaStream_t s);
     void (*gather_accepted)(const CandArgs& c, cudaStream_t s);
     void (*cut_accepted)(const CandArgs& c, int use_pivot, double pivot, uint64_t key_cut, cudaStream_t s);
     void (*commit)(const GridArgs& g, const CandArgs& c, cudaStream_t s);
-    void (*refine_mask)(const GridArgs& g, const RefineArgs& a, cudaStream_t s);
+    void (*refine_mask)(const GridArgs& g, const RefineArgs& a, int f32, cudaStream_t s);
     void (*refine_write)(const RefineArgs& a, cudaStream_t s);
     void (*check)(const GridArgs& g, unsigned long long* overlaps, unsigned long long* misplaced, cudaStream_t s);
     void (*volume_partials)(const GridArgs& g, double unit_volume, double* partials, int nblocks, cudaStream_t s);

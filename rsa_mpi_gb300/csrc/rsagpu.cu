@@ -154,6 +154,8 @@ struct SphereGrid {
     int32_t* head = nullptr;
     void release() {
         dfree(d_rows);
+        dfree(a.off);
+        dfree(a.radf);
         dfree(a.occ);
         dfree(a.pos);
         dfree(a.rad);
@@ -191,6 +193,8 @@ struct CandBuffers {
         dfree(a.blk);
         dfree(a.nblk);
         dfree(a.gather);
+        dfree(a.off);
+        dfree(a.kc);
         dfree(vidx);
         cap = 0;
     }
@@ -281,6 +285,10 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
         if (ncells > (int64_t)1 << 40) raise(RSAGPU_ERR_CAPACITY, "cell grid too large");
     }
     a.ncells = ncells;
+    for (int d = 0; d < D; d++) {
+        a.c[d] = c[d];
+        a.cf[d] = (float)c[d];
+    }
     const double R = 2 * rmax;
     int w[MAX_D];
     for (int d = 0; d < D; d++) {
@@ -360,6 +368,27 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
     a.occ = dalloc<uint32_t>(nwords);
     a.pos = dalloc<double>((uint64_t)ncells * D);
     a.rad = dalloc<double>(ncells);
+    a.off = dalloc<float>((uint64_t)ncells * D);
+    a.radf = dalloc<float>(ncells);
+    {
+        // Guard band of the FP32 screen: a bound, with a factor 4 to spare, on |FP32 model - FP64 value| of
+        // every squared distance the kernels compare.  Per dimension the model o c_f + (off_s - off_q)
+        // errs by at most E (float rounding of c, of the offsets, of the product and of the two sums, and of
+        // a voxel length); every difference is below A; the squares and the D-term sum add (D+1) roundings of
+        // a quantity below D A^2; the threshold (r_s + r_q)^2 in float adds 8 ulps of (2 r_max)^2.
+        const double u = std::ldexp(1.0, -24);
+        double cmax = 0;
+        int wmax = 0;
+        for (int d = 0; d < D; d++) {
+            cmax = std::max(cmax, c[d]);
+            wmax = std::max(wmax, w[d]);
+        }
+        const double lmax = (rmax + rmin) / std::sqrt((double)D);  // level-0 voxel length bound
+        const double E = u * cmax * (4 * wmax + 8) + u * lmax;
+        const double Amax = (wmax + 1) * cmax + lmax;
+        const double G = 4 * (D * E * (2 * Amax + E) + (D + 1) * u * D * Amax * Amax + 8 * u * (2 * rmax) * (2 * rmax));
+        a.guard = (float)G;
+    }
     a.phase = dalloc<int32_t>(ncells);
     G.head = dalloc<int32_t>(ncells);
     CK(cudaMemset(a.occ, 0, nwords * sizeof(uint32_t)));
@@ -393,6 +422,8 @@ void ensure_cand(rsagpu_algo* A, uint64_t n) {
     C.a.blk = dalloc<int32_t>(cap * NB);
     C.a.nblk = dalloc<uint8_t>(cap);
     C.a.gather = dalloc<uint64_t>(cap);
+    C.a.off = dalloc<float>(cap * D);
+    C.a.kc = dalloc<int32_t>(cap * D);
     C.vidx = dalloc<uint64_t>(cap);
     C.cap = cap;
 }
@@ -480,20 +511,23 @@ void refine(rsagpu_algo* A) {
     r.err = A->d_err;
     r.survivors = A->d_err + 1;
     r.visits = A->d_visits;
+    r.retests = A->d_visits + 1;
     CK(cudaMemsetAsync(r.survivors, 0, sizeof(uint32_t), A->stream));
-    CK(cudaMemsetAsync(r.visits, 0, sizeof(unsigned long long), A->stream));
+    CK(cudaMemsetAsync(r.visits, 0, 2 * sizeof(unsigned long long), A->stream));
     const uint64_t nb = (A->V + 31) / 32;  // warps
     CK(cudaEventRecord(A->ev[8], A->stream));
-    A->ops->refine_mask(A->dom->grid.a, r, A->stream);
+    A->ops->refine_mask(A->dom->grid.a, r, A->form == RSAGPU_FORM_FP32_GUARD, A->stream);
     CK(cudaEventRecord(A->ev[9], A->stream));
     launch_scan_blocks(A->block_counts, A->block_offsets, nb, nullptr, A->stream);
     uint64_t total = 0;
     uint32_t survivors = 0;
-    unsigned long long visits = 0;
+    unsigned long long visits = 0, retests = 0;
+    CK(cudaMemcpyAsync(&retests, r.retests, sizeof(unsigned long long), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaMemcpyAsync(&total, A->block_offsets + nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaMemcpyAsync(&survivors, r.survivors, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaMemcpyAsync(&visits, r.visits, sizeof(unsigned long long), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaStreamSynchronize(A->stream));
+    A->stats.retests += retests;
     {
         // the mask pass of this launch: its device time and algorithmic bytes (each logical element once:
         // parent coordinates, stencil occupancy bits up to the grid size, visited spheres up to the
@@ -594,10 +628,11 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
     A->heads_dirty = true;
     CandArgs c = cand_args(A, n);
     const DimOps* ops = A->ops;
+    const int f32 = A->form == RSAGPU_FORM_FP32_GUARD;
     ev_record(A, 2);
-    ops->probe(g, c, A->stream);
+    ops->probe(g, c, f32, A->stream);
     ev_record(A, 3);
-    ops->collect(g, c, A->stream);
+    ops->collect(g, c, f32, A->stream);
     ev_record(A, 10);
     if (A->timing) {
         CK(cudaEventSynchronize(A->ev[10]));
@@ -610,7 +645,7 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
         ev_record(A, 10);
         for (int b = 0; b < batch; b++, it++) {
             if (it > MAX_SETTLE) raise(RSAGPU_ERR_NO_PROGRESS, "settle did not converge in %d iterations", MAX_SETTLE);
-            ops->settle(g, c, it, A->stream);
+            ops->settle(g, c, it, f32, A->stream);
         }
         ev_record(A, 11);
         CK(cudaMemcpyAsync(A->h_counters + COUNTERS + it - 1, c.und + it - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -658,8 +693,9 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
     ops->commit(g, c, A->stream);
     A->heads_dirty = false;
     ev_record(A, 5);
-    CK(cudaMemcpyAsync(A->h_counters, c.counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
+    CK(cudaMemcpyAsync(A->h_counters, c.counters, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaStreamSynchronize(A->stream));
+    A->stats.retests += A->h_counters[4];
     if (A->h_counters[2] & ERR_DOUBLE_OCCUPANCY)
         raise(RSAGPU_ERR_INVARIANT, "two accepted centres in one grid cell");
     (void)keep_state;
@@ -1020,9 +1056,11 @@ int rsagpu_algo_create(rsagpu_domain* dom, const rsagpu_radgen* rg, int nbshots,
             for (auto& e : A->ev) CK(cudaEventCreate(&e));
             A->d_err = dalloc<uint32_t>(2);
             CK(cudaMemset(A->d_err, 0, 2 * sizeof(uint32_t)));
-            A->d_visits = dalloc<unsigned long long>(1);
+            A->d_visits = dalloc<unsigned long long>(2);
             // the algo rebuilds the domain's grid and drops its spheres (operator_algorithm.ixx:25-26)
             build_grid(dom, rg->rmin(), std::max(rg->rmax(), 0.0));
+            dom->grid.a.mono = rg->r.size() == 1;
+            dom->grid.a.rmono = rg->r.front();
             A->placed = 0;
             ensure_cand(A, 1024);
         } catch (...) {
@@ -1114,6 +1152,10 @@ int rsagpu_algo_reset_radgen(rsagpu_algo* algo, const rsagpu_radgen* rg) {
         algo->rg = *rg;
         algo->rg.idx = 0;
         algo->begun = false;
+        // spheres of the previous generator keep their radii: the grid's one-radius shortcut holds only if
+        // the new generator has the same single radius
+        GridArgs& ga = algo->dom->grid.a;
+        ga.mono = ga.mono && rg->r.size() == 1 && rg->r.front() == ga.rmono;
     });
 }
 

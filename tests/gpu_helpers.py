@@ -23,7 +23,7 @@ def sort_voxels(v):
     return v[np.lexsort(tuple(v[:, d] for d in reversed(range(v.shape[1]))))]
 
 
-def make_pair(case, cap_exact=False):
+def make_pair(case, cap_exact=False, form=0):
     """(oracle, gpu algo, gpu domain) for a golden case."""
     D = case["dim"]
     vol = 1.0 if case["volume_mode"] == 1 else float(np.prod(case["L"]))
@@ -34,15 +34,16 @@ def make_pair(case, cap_exact=False):
     rg = RadiusGenerator(D, classes, volume=vol)
     dom = Domain([0.0] * D, case["L"], rg.max_radius)
     algo = Algo(dom, rg, case["nbshots"])
+    algo.set_form(form)
     if cap_exact:
         algo.set_cap_rule(_lib.RSAGPU_CAP_EXACT)
     return ora, algo, dom
 
 
-def lockstep(case, seed, cap_exact=False, check_voxels=True, max_rounds=100000):
+def lockstep(case, seed, cap_exact=False, check_voxels=True, max_rounds=100000, form=0):
     """Drives the oracle and the GPU with the reference's own candidate stream; asserts equal decisions
     every round and equal voxel sets after every refinement.  Returns (oracle, algo, dom, rounds)."""
-    ora, algo, dom = make_pair(case, cap_exact)
+    ora, algo, dom = make_pair(case, cap_exact, form)
     ora.begin(seed)
     algo.begin()
     rounds = 0

@@ -40,6 +40,22 @@ def test_product_run_is_valid_maximal_and_matches_fraction(dim, L, r, phi_ref, t
     assert abs(phi - phi_ref) < tol, (phi, phi_ref)
 
 
+@pytest.mark.parametrize("dim,L,r", [(2, [1.0, 1.0], 0.005), (3, [1.0, 1.0, 1.0], 0.01), (3, [0.9, 1.1, 1.0], 0.013)])
+def test_fp32_guard_form_gives_the_fp64_form_output(dim, L, r):
+    """The FP32 screen decides only outside the guard band and retests the rest in FP64: same spheres."""
+    out = []
+    for form in (_lib.RSAGPU_FORM_FP64, _lib.RSAGPU_FORM_FP32_GUARD):
+        rg = RadiusGenerator(dim, [(r, 1.0, 0)], volume=float(np.prod(L)))
+        dom = Domain([0.0] * dim, L, r)
+        algo = Algo(dom, rg, 6000)
+        algo.set_form(form)
+        algo.proceed(11)
+        out.append((dom.arrays()[0], algo.stats()))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert out[0][1]["retests"] == 0 and out[1][1]["retests"] > 0
+    assert out[1][1]["maximal"] == 1
+
+
 def test_product_runs_are_deterministic_per_seed():
     d1, _ = run_product(2, [1.0, 1.0], 0.01, 3)
     d2, _ = run_product(2, [1.0, 1.0], 0.01, 3)

@@ -17,11 +17,12 @@ pytestmark = pytest.mark.gpu
 MONO = ["c1_2d_r0.005_s0", "t2d_r0.05_s0", "t3d_r0.05_s0", "k3d_r0.02_s1", "t3d_box3.5_r0.4_s0", "n2d_rect_s7"]
 
 
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
 @pytest.mark.parametrize("name", MONO)
-def test_replay_reproduces_reference_output(name):
+def test_replay_reproduces_reference_output(name, form):
     case = INDEX[name]
     g = np.load(f"{GOLDEN}/{name}.npz")
-    ora, algo, dom, rounds = lockstep(case, case["seed"])
+    ora, algo, dom, rounds = lockstep(case, case["seed"], form=form)
     assert rounds == len(g["shots"])
     pos, rad, ph = sort_spheres(*dom.arrays())
     np.testing.assert_array_equal(pos, g["centers"])
@@ -32,11 +33,12 @@ def test_replay_reproduces_reference_output(name):
     assert len(algo.voxels()[0]) == 0
 
 
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
 @pytest.mark.parametrize("name", ["p2d_poly_s3", "t3d_radius_s0", "p3d_poly_small_s2"])
-def test_replay_polydisperse_exact_cap(name):
+def test_replay_polydisperse_exact_cap(name, form):
     """Class counts reached inside a round: both sides keep exactly the remaining count."""
     case = INDEX[name]
-    ora, algo, dom, rounds = lockstep(case, case["seed"], cap_exact=True)
+    ora, algo, dom, rounds = lockstep(case, case["seed"], cap_exact=True, form=form)
     po, ro, fo = sort_spheres(*ora.spheres())
     pg, rg, fg = sort_spheres(*dom.arrays())
     np.testing.assert_array_equal(po, pg)
