@@ -104,7 +104,10 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def run_gpu_step(dim, L, r, seed, form=0):
+FORM_NAMES = {0: "plain FP64", 1: "FP32 screen + FP64 guard-band retest"}
+
+
+def run_gpu_step(dim, L, r, seed, form=1):
     from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator
     rg = RadiusGenerator(dim, [(r, 1.0, 0)], volume=float(math.prod(L)))
     dom = Domain([0.0] * dim, L, r)
@@ -119,7 +122,7 @@ def run_gpu_step(dim, L, r, seed, form=0):
     return n, st, ms, by
 
 
-def run_e2e_step(dim, L, r, seed):
+def run_e2e_step(dim, L, r, seed, form=1):
     """The user's call through the C ABI with host buffers: returns (spheres, seconds, d2h bytes, h2d bytes)."""
     import ctypes as C
     import numpy as np
@@ -138,6 +141,7 @@ def run_e2e_step(dim, L, r, seed):
                                                  1, float(np.prod(sup)), 0.0, C.byref(rg)))
     algo = C.c_void_p()
     _lib.check(Lb.rsagpu_algo_create(dom, rg, 6000, C.byref(algo)))
+    _lib.check(Lb.rsagpu_algo_set_form(algo, form, 0))
     _lib.check(Lb.rsagpu_algo_proceed(algo, seed))
     n = C.c_uint64()
     _lib.check(Lb.rsagpu_domain_extract(dom, None, None, None, 0, C.byref(n)))
@@ -213,6 +217,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", type=int, default=1, choices=[0, 1], help="0 = plain FP64, 1 = FP32 + guard band")
+    ap.add_argument("--no-forms", action="store_true", help="skip the per-form comparison runs")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -231,7 +237,7 @@ def main():
     dim, L, r, seed0, desc = WORKLOADS[args.workload]
     seed = seed0 + rank  # each rank samples an independent instance (replicas)
     for _ in range(args.warmup):
-        run_gpu_step(dim, L, r, seed)
+        run_gpu_step(dim, L, r, seed, args.form)
 
     def barrier():
         torch.cuda.synchronize()
@@ -246,7 +252,7 @@ def main():
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            n, st, ms, by = run_gpu_step(dim, L, r, seed)
+            n, st, ms, by = run_gpu_step(dim, L, r, seed, args.form)
             spheres += n
             dev_ms += st["ms_total"]
             mask_ms += list(ms)
@@ -256,10 +262,23 @@ def main():
         wall = time.perf_counter() - t0
     launches = kernel_launches() - launches0
 
+    # the other forms on the same GPU, one run each (outside the timed region)
+    forms = {}
+    if not args.no_forms:
+        primary = {"spheres_per_s": spheres / (dev_ms * 1e-3), "ms": dev_ms / args.steps, "retests": stats["retests"]}
+        forms[FORM_NAMES[args.form]] = primary
+        other = 1 - args.form
+        n2, st2, _, _ = run_gpu_step(dim, L, r, seed, other)
+        forms[FORM_NAMES[other]] = {"spheres_per_s": n2 / (st2["ms_total"] * 1e-3), "ms": st2["ms_total"],
+                                    "retests": st2["retests"], "same_spheres": n2 == spheres // max(1, args.steps)}
+        base = forms[FORM_NAMES[0]]["spheres_per_s"]
+        for v in forms.values():
+            v["speedup_vs_fp64"] = v["spheres_per_s"] / base
+
     # e2e through the C ABI with host buffers
     e2e_n, e2e_s, d2h = 0, 0.0, 0
     for _ in range(max(1, args.steps)):
-        k, s, b = run_e2e_step(dim, L, r, seed)
+        k, s, b = run_e2e_step(dim, L, r, seed, args.form)
         e2e_n += k
         e2e_s += s
         d2h = b
@@ -298,19 +317,20 @@ def main():
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "f64" if args.form == 0 else "f32/f64",
         "data": "synthetic",
-        "config": {"workload": desc, "form": "plain FP64", "spheres_per_step": spheres // max(1, args.steps),
+        "config": {"workload": desc, "form": FORM_NAMES[args.form], "spheres_per_step": spheres // max(1, args.steps),
                    "parallelism": f"replicas x{world}", "l2": "working set > L2 (no flush needed)"},
         "wall_ms_per_step": wall_max * 1e3 / args.steps,
-        "roofline": {"bound": "hbm", "kernel": "k_refine_mask", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": "k_refine_mask32" if args.form == 1 else "k_refine_mask", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "share_of_step": float(mm.sum() / max(dev_ms, 1e-9)),
                      "launches": int(len(mm)), "algorithmic_bytes_per_launch": float(mb.mean()) if len(mb) else 0.0},
         "e2e": {"value": e2e_all / e2e_max, "unit": "spheres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "stats": {k: stats[k] for k in ("rounds", "refinements", "darts", "settle_iterations", "peak_voxels", "final_level",
-                                         "maximal")},
+                                         "maximal", "retests")},
+        "forms": forms,
     }
     cs = clocks.summary()
     if cs:

@@ -52,6 +52,9 @@ __host__ __device__ inline Grid<D> make_grid(const GridArgs& a) {
     g.S = a.S;
     g.rows = a.rows;
     g.R = a.R;
+    g.rows_r2 = a.rows_r2;
+    g.c0f = (float)(1.0 / a.inv_c[0]);
+    g.rmax = a.rmax;
     g.off = a.off;
     g.radf = a.radf;
     for (int d = 0; d < D; d++) {
@@ -165,7 +168,7 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
         cell_of<D>(g, geo, x, k);
         bool hit;
         if constexpr (!F32) {
-            hit = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
+            hit = visit_placed<D>(g, geo, k, search_r2(r, g.rmax), [&](int64_t, const double* img, double rs) {
                 return collide64<D>(r, x, rs, img);
             });
         } else {
@@ -179,7 +182,7 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
                 c.kc[(uint64_t)i * D + d] = k[d];
             }
             const float rf = __double2float_rn(r);
-            hit = visit_placed_o<D>(g, k, [&](int64_t idx, const int32_t* o, const int8_t* q) {
+            hit = visit_placed_o<D>(g, k, search_r2(r, g.rmax), [&](int64_t idx, const int32_t* o, const int8_t* q) {
                 const float rs = g.mono ? g.rmonof : g.radf[idx];
                 const float R = __fadd_rn(rf, rs);
                 const float R2 = __fmul_rn(R, R);
@@ -217,8 +220,8 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
 // Visits the same-round candidates in the stencil around cell k (linked lists head/next).
 template <class F>
 __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c,
-                                                 const int32_t* k, F&& f) {
-    walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
+                                                 const int32_t* k, float R2q, F&& f) {
+    walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.c0f, R2q, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
         for (int32_t x = lo; x <= hi; x++) {
             for (int32_t j = c.head[base + x]; j >= 0; j = c.next[j]) {
                 double p[D], img[D];
@@ -234,8 +237,9 @@ __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>&
 
 // Same walk with the integer cell offset o of each candidate (FP32 screen); f(j, o, q).
 template <class F>
-__device__ __forceinline__ void visit_candidates_o(const Grid<D>& g, const CandArgs& c, const int32_t* k, F&& f) {
-    walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
+__device__ __forceinline__ void visit_candidates_o(const Grid<D>& g, const CandArgs& c, const int32_t* k, float R2q,
+                                                   F&& f) {
+    walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.c0f, R2q, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
         int32_t o[D];
 #pragma unroll
         for (int d = 1; d < D; d++) o[d] = row[1 + d];
@@ -309,7 +313,7 @@ __global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
         if constexpr (!F32) {
             int32_t k[D];
             cell_of<D>(g, geo, x, k);
-            visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
+            visit_candidates(g, geo, c, k, search_r2(r, g.rmax), [&](int32_t j, const double* img) {
                 if (!precedes(c.key[j], j, key, i)) return false;
                 if (collide64<D>(r, x, c.rad[j], img)) record(j);
                 return false;
@@ -323,7 +327,7 @@ __global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
                 offq[d] = c.off[(uint64_t)i * D + d];
             }
             const float rf = __double2float_rn(r);
-            visit_candidates_o(g, c, k, [&](int32_t j, const int32_t* o, const int8_t* q) {
+            visit_candidates_o(g, c, k, search_r2(r, g.rmax), [&](int32_t j, const int32_t* o, const int8_t* q) {
                 if (!precedes(c.key[j], j, key, i)) return false;
                 if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) record(j);
                 return false;
@@ -377,7 +381,7 @@ __global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
                     if constexpr (!F32) {
                         int32_t k[D];
                         cell_of<D>(g, geo, x, k);
-                        visit_candidates(g, geo, c, k, [&](int32_t j, const double* img) {
+                        visit_candidates(g, geo, c, k, search_r2(r, g.rmax), [&](int32_t j, const double* img) {
                             if (!precedes(c.key[j], j, key, i)) return false;
                             if (collide64<D>(r, x, c.rad[j], img)) judge(j);
                             return any_acc;
@@ -391,7 +395,7 @@ __global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
                             offq[d] = c.off[(uint64_t)i * D + d];
                         }
                         const float rf = __double2float_rn(r);
-                        visit_candidates_o(g, c, k, [&](int32_t j, const int32_t* o, const int8_t* q) {
+                        visit_candidates_o(g, c, k, search_r2(r, g.rmax), [&](int32_t j, const int32_t* o, const int8_t* q) {
                             if (!precedes(c.key[j], j, key, i)) return false;
                             if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) judge(j);
                             return any_acc;
@@ -583,7 +587,8 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
         uint64_t preR2[K_PRE];
         int npre = 0;
         bool overflow = false;
-        const bool covered = visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
+        const float R2q = search_r2(p.rmin, g.rmax);
+        const bool covered = visit_placed<D>(g, geo, k, R2q, [&](int64_t, const double* img, double rs) {
             visits++;
             const double R = __dadd_rn(rs, p.rmin);
             const uint64_t R2b = dbits(__dmul_rn(R, R));
@@ -638,7 +643,7 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
                 // the list was full: test every prefilter sphere again, straight from the grid
                 cov[0] = 0;
                 for (int w = 1; w < MASK_WORDS; w++) cov[w] = 0;
-                visit_placed<D>(g, geo, k, [&](int64_t, const double* img, double rs) {
+                visit_placed<D>(g, geo, k, R2q, [&](int64_t, const double* img, double rs) {
                     const double R = __dadd_rn(rs, p.rmin);
                     const uint64_t R2b = dbits(__dmul_rn(R, R));
                     double dl0[D], dl1[D], s = 0.0;
@@ -733,7 +738,8 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask32(Grid<D> g, Geo<D
             const double R = __dadd_rn(g.mono ? g.rmono : g.rad[idx], p.rmin);
             return dbits(__dmul_rn(R, R));
         };
-        const bool covered = visit_placed_o<D>(g, k, [&](int64_t idx, const int32_t* o, const int8_t* q) {
+        const float R2q = search_r2(p.rmin, g.rmax);
+        const bool covered = visit_placed_o<D>(g, k, R2q, [&](int64_t idx, const int32_t* o, const int8_t* q) {
             visits++;
             const float rs = g.mono ? g.rmonof : g.radf[idx];
             const float R = __fadd_rn(rs, p.rminf);
@@ -839,7 +845,7 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask32(Grid<D> g, Geo<D
                 // the list was full: every prefilter sphere again, in FP64, straight from the grid
 #pragma unroll
                 for (int w = 0; w < MASK_WORDS; w++) cov[w] = 0;
-                visit_placed<D>(g, geo, k, [&](int64_t idx, const double* img, double rs) {
+                visit_placed<D>(g, geo, k, R2q, [&](int64_t idx, const double* img, double rs) {
                     const double R = __dadd_rn(rs, p.rmin);
                     const uint64_t R2b = dbits(__dmul_rn(R, R));
                     double dl0[D], dl1[D], ss = 0.0;
@@ -938,7 +944,7 @@ __global__ void k_check(Grid<D> g, Geo<D> geo, unsigned long long* overlaps, uns
         rem /= g.n[d];
     }
     unsigned long long cnt = 0;
-    visit_placed<D>(g, geo, kc, [&](int64_t j, const double* img, double rs) {
+    visit_placed<D>(g, geo, kc, search_r2(r, g.rmax), [&](int64_t j, const double* img, double rs) {
         if (j > idx && collide64<D>(r, x, rs, img)) cnt++;
         return false;
     });

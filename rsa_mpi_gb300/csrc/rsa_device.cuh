@@ -51,6 +51,9 @@ struct Grid {
     // the same stencil as rows along dimension 0: row r = {xlo, xhi, o_1, ..., o_{D-1}} (D+1 int8)
     const int8_t* rows;
     int R;
+    const float* rows_r2;  // per row: squared distance to its nearest cell along dimensions 1..D-1 (rows sorted by it)
+    float c0f;             // cell edge along dimension 0
+    double rmax;           // largest radius the grid holds
     // FP32 screening representation of the placed centres (guard-band form): off = centre minus the
     // corner of its cell, rounded to float; radf = radius rounded to float
     const float* off;
@@ -182,9 +185,15 @@ __device__ __forceinline__ uint32_t occ_bits(const uint32_t* occ, int64_t lin, i
 // three contiguous segments along dimension 0 (left wrap, inside, right wrap).  g(base, lo, hi, q, row) is
 // called per segment [lo, hi] with the image shifts q; it returns true to stop.
 template <int D, class G>
-__device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, int R, const int32_t* k, G&& g) {
+__device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, int R, const float* rows_r2, float c0f,
+                                          float R2q, const int32_t* k, G&& g) {
     for (int r = 0; r < R; r++) {
+        // only cells that may hold a point within sqrt(R2q) of the query cell: rows by nearest distance, and
+        // along dimension 0 the offsets |o_0| <= 1 + sqrt(R2q - row distance) / c0
+        const float rest = rows_r2[r];
+        if (rest > R2q) break;
         const int8_t* row = rows + r * (D + 1);
+        const int32_t o0max = 1 + (int32_t)(sqrtf(R2q - rest) / c0f);
         int8_t q[D];
         int64_t base = 0;
 #pragma unroll
@@ -197,7 +206,7 @@ __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, 
             base = base * n[d] + kk;
         }
         base *= n[0];
-        const int32_t a = k[0] + (int32_t)row[0], b = k[0] + (int32_t)row[1];
+        const int32_t a = k[0] + max((int32_t)row[0], -o0max), b = k[0] + min((int32_t)row[1], o0max);
         if (a < 0) {
             q[0] = -1;
             if (g(base, a + n[0], (b < 0 ? b : -1) + n[0], q, row)) return true;
@@ -217,8 +226,8 @@ __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, 
 
 // Visits the placed spheres in the stencil around cell k; f(idx, img, r) returns true to stop.
 template <int D, class F>
-__device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo, const int32_t* k, F&& f) {
-    return walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
+__device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo, const int32_t* k, float R2q, F&& f) {
+    return walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.c0f, R2q, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
         for (int32_t x = lo; x <= hi; x += 32) {
             const int len = hi - x + 1 < 32 ? hi - x + 1 : 32;
             uint32_t bits = occ_bits(g.occ, base + x, len);
@@ -240,8 +249,8 @@ __device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo
 // Visits the placed spheres in the stencil around cell k with their integer cell offset o (the periodic
 // shift folded in: o = cell of the image - k); f(idx, o, q) returns true to stop.
 template <int D, class F>
-__device__ __forceinline__ bool visit_placed_o(const Grid<D>& g, const int32_t* k, F&& f) {
-    return walk_rows<D>(g.n, g.rows, g.R, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
+__device__ __forceinline__ bool visit_placed_o(const Grid<D>& g, const int32_t* k, float R2q, F&& f) {
+    return walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.c0f, R2q, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
         int32_t o[D];
 #pragma unroll
         for (int d = 1; d < D; d++) o[d] = row[1 + d];
@@ -275,6 +284,12 @@ __device__ __forceinline__ float sumsq32(const float* v) {
 #pragma unroll
     for (int d = 0; d < D; d++) s = __fadd_rn(s, __fmul_rn(v[d], v[d]));
     return s;
+}
+
+// squared search radius (r_query + r_max)^2 with a margin, as float
+__device__ __forceinline__ float search_r2(double rq, double rmax) {
+    const float s = (float)(rq + rmax);
+    return s * s * 1.0001f;
 }
 
 // Bit patterns of non-negative doubles order like the values: integer max / compare on the ALU

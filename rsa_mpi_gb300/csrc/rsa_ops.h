@@ -24,6 +24,8 @@ struct GridArgs {
     int S;
     const int8_t* rows;  // stencil rows along dimension 0: {xlo, xhi, o_1, ..., o_{D-1}}
     int R;
+    const float* rows_r2;  // per row: squared nearest distance along dimensions 1..D-1 (rows sorted by it)
+    double rmax;           // largest radius the grid holds
     float* off;          // FP32 screening offsets (D floats per cell)
     float* radf;         // radii rounded to float
     double c[MAX_D];     // cell edge

@@ -151,9 +151,11 @@ struct SphereGrid {
     std::vector<int8_t> rows;
     int8_t* d_stencil = nullptr;
     int8_t* d_rows = nullptr;
+    float* d_rows_r2 = nullptr;
     int32_t* head = nullptr;
     void release() {
         dfree(d_rows);
+        dfree(d_rows_r2);
         dfree(a.off);
         dfree(a.radf);
         dfree(a.occ);
@@ -356,12 +358,31 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
                 rows.push_back(r);
             }
         }
+        auto rest2 = [&](const std::vector<int8_t>& r) {
+            double s2 = 0;
+            for (int d = 1; d < D; d++) {
+                const double t = std::max(0, std::abs((int)r[1 + d]) - 1) * c[d];
+                s2 += t * t;
+            }
+            return s2;
+        };
+        std::stable_sort(rows.begin(), rows.end(), [&](const std::vector<int8_t>& x, const std::vector<int8_t>& y) {
+            return rest2(x) < rest2(y);
+        });
         G.rows.clear();
-        for (auto& r : rows) G.rows.insert(G.rows.end(), r.begin(), r.end());
+        std::vector<float> r2;
+        for (auto& r : rows) {
+            G.rows.insert(G.rows.end(), r.begin(), r.end());
+            r2.push_back((float)(rest2(r) * (1 - 1e-6)));  // rounded down: never drops a needed row
+        }
         a.R = (int)rows.size();
         G.d_rows = dalloc<int8_t>(G.rows.size());
         CK(cudaMemcpy(G.d_rows, G.rows.data(), G.rows.size(), cudaMemcpyHostToDevice));
         a.rows = G.d_rows;
+        G.d_rows_r2 = dalloc<float>(r2.size());
+        CK(cudaMemcpy(G.d_rows_r2, r2.data(), r2.size() * sizeof(float), cudaMemcpyHostToDevice));
+        a.rows_r2 = G.d_rows_r2;
+        a.rmax = rmax;
     }
     // one padding word: the two-word window of occ_bits reads up to word nwords
     const int64_t nwords = (ncells + 31) / 32 + 1;
@@ -537,9 +558,10 @@ void refine(rsagpu_algo* A) {
         const GridArgs& g = A->dom->grid.a;
         const double bits = std::min<double>((double)A->V * g.S, (double)g.ncells);
         const double sph = std::min<double>((double)visits, (double)A->placed);
+        // bytes per visited sphere: FP64 centre + radius, or FP32 offsets (+ FP32 radius unless one class)
+        const double per_sphere = A->form == RSAGPU_FORM_FP32_GUARD ? 4.0 * D + (g.mono ? 0 : 4) : 8.0 * D + (g.mono ? 0 : 8);
         A->mask_ms.push_back(ms);
-        A->mask_bytes.push_back((double)A->V * 8 * D + bits / 8 + sph * (8.0 * D + 8) +
-                                (double)A->V * 4 * A->ops->mask_words);
+        A->mask_bytes.push_back((double)A->V * 8 * D + bits / 8 + sph * per_sphere + (double)A->V * 4 * A->ops->mask_words);
     }
     if (survivors == 0) {
         // remove_covered emptied the list: subdivide_uncovered returns before halving the length
