@@ -136,6 +136,13 @@ int rsagpu_algo_stats(rsagpu_algo* algo, rsagpu_stats* out);
  * on the algo's stream around the launch) and algorithmic bytes (parent coordinates, stencil occupancy
  * bits up to the grid size, visited spheres up to the spheres placed, child masks). */
 int rsagpu_algo_kernel_profile(rsagpu_algo* algo, double* ms, double* bytes, uint64_t cap, uint64_t* n_out);
+/* Learned schedule training data: after each pass the schedule's decision is flipped with probability
+ * epsilon (host RNG seeded with seed).  0 = off (default). */
+int rsagpu_algo_set_exploration(rsagpu_algo* algo, double epsilon, uint64_t seed);
+/* Per round of the last proceed(): the 16 state features the schedule saw, whether it refined, and the
+ * host wall time of the pass and of the refinement that followed. */
+int rsagpu_algo_trace_features(rsagpu_algo* algo, float* features, uint8_t* refined, double* pass_ms,
+                               double* refine_ms, uint64_t cap, uint64_t* n_out);
 /* Turns per-kernel CUDA-event timing on (1) or off (0, default). */
 int rsagpu_algo_set_timing(rsagpu_algo* algo, int on);
 

@@ -88,6 +88,8 @@ _SIGS = {
     "rsagpu_algo_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "rsagpu_algo_set_timing": (C.c_int, [_vp, C.c_int]),
     "rsagpu_algo_kernel_profile": (C.c_int, [_vp, _d, _d, C.c_uint64, _u64]),
+    "rsagpu_algo_set_exploration": (C.c_int, [_vp, C.c_double, C.c_uint64]),
+    "rsagpu_algo_trace_features": (C.c_int, [_vp, _f32, _u8, _d, _d, C.c_uint64, _u64]),
     "rsagpu_algo_begin": (C.c_int, [_vp]),
     "rsagpu_algo_replay_round": (C.c_int, [_vp, C.c_uint64, _d, _u64, _d, _i32, C.c_uint64, C.c_int, _u8, _u64]),
     "rsagpu_algo_end_round": (C.c_int, [_vp, C.c_uint64, C.c_uint64, _i32, _i32]),

@@ -205,6 +205,7 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
             const int64_t idx = cell_index<D>(g, k);
             c.cell[i] = idx;
             c.next[i] = atomicExch(c.head + idx, (int32_t)i);
+            atomicOr(c.cocc + (idx >> 5), 1u << (idx & 31));
             alive = true;
         }
     }
@@ -222,13 +223,19 @@ template <class F>
 __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c,
                                                  const int32_t* k, float R2q, F&& f) {
     walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.c0f, R2q, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
-        for (int32_t x = lo; x <= hi; x++) {
-            for (int32_t j = c.head[base + x]; j >= 0; j = c.next[j]) {
-                double p[D], img[D];
+        for (int32_t x = lo; x <= hi; x += 32) {
+            const int len = hi - x + 1 < 32 ? hi - x + 1 : 32;
+            uint32_t bits = occ_bits(c.cocc, base + x, len);  // cells holding a candidate of this round
+            while (bits) {
+                const int jj = __ffs(bits) - 1;
+                bits &= bits - 1;
+                for (int32_t j = c.head[base + x + jj]; j >= 0; j = c.next[j]) {
+                    double p[D], img[D];
 #pragma unroll
-                for (int d = 0; d < D; d++) p[d] = c.pos[(uint64_t)j * D + d];
-                image_of<D>(geo, p, q, img);
-                if (f(j, img)) return true;
+                    for (int d = 0; d < D; d++) p[d] = c.pos[(uint64_t)j * D + d];
+                    image_of<D>(geo, p, q, img);
+                    if (f(j, img)) return true;
+                }
             }
         }
         return false;
@@ -244,10 +251,16 @@ __device__ __forceinline__ void visit_candidates_o(const Grid<D>& g, const CandA
 #pragma unroll
         for (int d = 1; d < D; d++) o[d] = row[1 + d];
         const int32_t shift0 = (q[0] < 0 ? -g.n[0] : (q[0] > 0 ? g.n[0] : 0)) - k[0];
-        for (int32_t x = lo; x <= hi; x++) {
-            o[0] = x + shift0;
-            for (int32_t j = c.head[base + x]; j >= 0; j = c.next[j])
-                if (f(j, o, q)) return true;
+        for (int32_t x = lo; x <= hi; x += 32) {
+            const int len = hi - x + 1 < 32 ? hi - x + 1 : 32;
+            uint32_t bits = occ_bits(c.cocc, base + x, len);
+            while (bits) {
+                const int jj = __ffs(bits) - 1;
+                bits &= bits - 1;
+                o[0] = x + jj + shift0;
+                for (int32_t j = c.head[base + x + jj]; j >= 0; j = c.next[j])
+                    if (f(j, o, q)) return true;
+            }
         }
         return false;
     });
@@ -453,6 +466,7 @@ __global__ void k_commit(Grid<D> g, Geo<D> geo, CandArgs c) {
         const uint32_t i = c.alive[t];
         const int64_t idx = c.cell[i];
         c.head[idx] = -1;
+        atomicAnd(c.cocc + (idx >> 5), ~(1u << (idx & 31)));
         if (c.state[i] == ST_ACCEPTED) {
             acc = true;
             const uint32_t bit = 1u << (idx & 31);

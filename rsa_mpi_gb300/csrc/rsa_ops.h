@@ -45,6 +45,7 @@ struct CandArgs {
     uint8_t* state;     // ST_*
     int32_t* next;      // linked list of candidates per cell
     int32_t* head;      // per grid cell, -1 = no candidate
+    uint32_t* cocc;     // 1 bit per grid cell: holds a candidate of this round (one padding word)
     uint32_t* alive;    // candidates that survived the probe
     uint32_t* counters; // [0] = alive, [1] = accepted, [2] = error bits, [3] = gathered, [4] = FP64 retests
     float* off;         // FP32 screening offsets of the candidates (guard-band form)
@@ -112,6 +113,8 @@ uint64_t kernel_launch_count();
 void count_launch(int n = 1);
 // text returned by rsagpu_last_error() for the calling thread
 void set_last_error(const char* msg);
+// learned schedule: y[0..1] = MLP(features[0..15]) on stream s (mlp.cu)
+int mlp_decide(const uint16_t* d_weights, const float* d_features, float* d_out, cudaStream_t s);
 
 constexpr int REFINE_BLOCK = 256;
 constexpr int OCC_BLOCK = 256;  // words per extract block

@@ -5,7 +5,9 @@
 // (operator_ghost, rsa_ghost_area, rsa_buffer) becomes periodic index wrap inside the kernels and its
 // Allreduce counters become device counters read once per round.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <random>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -122,7 +124,12 @@ struct TraceRow {
     uint64_t voxels, darts, accepted;
     uint8_t refined;
     int32_t level;
+    float features[16];  // state seen by the schedule after the round's pass
+    double pass_ms;      // host wall time of the pass (darts to commit)
+    double refine_ms;    // host wall time of the refinement that followed (0 if none)
 };
+
+constexpr int NFEAT = 16;
 
 constexpr int MAX_SETTLE = 4096;
 constexpr int COUNTERS = 8;
@@ -153,7 +160,9 @@ struct SphereGrid {
     int8_t* d_rows = nullptr;
     float* d_rows_r2 = nullptr;
     int32_t* head = nullptr;
+    uint32_t* cocc = nullptr;  // candidate occupancy bits of the current round
     void release() {
+        dfree(cocc);
         dfree(d_rows);
         dfree(d_rows_r2);
         dfree(a.off);
@@ -230,9 +239,19 @@ struct rsagpu_algo {
     uint32_t* h_counters = nullptr;  // pinned mirror: COUNTERS + MAX_SETTLE + 1
     // schedule
     int form = RSAGPU_FORM_FP64, schedule = RSAGPU_SCHEDULE_HEURISTIC, cap_rule = RSAGPU_CAP_REFERENCE;
-    double factor = 1.0, miss_thr = -1.0;
-    uint64_t min_darts = 4096, max_darts = 1ull << 25;
+    // heuristic defaults tuned on config 2 (a sweep of factor x threshold): a quarter dart per voxel per pass,
+    // refine when 99% of the darts miss
+    double factor = 0.25, miss_thr = 0.99;
+    uint64_t min_darts = 4096, max_darts = 1ull << 26;
     std::vector<uint16_t> mlp;
+    uint16_t* d_mlp = nullptr;      // the weights on the device
+    float* d_feat = nullptr;        // features in, two outputs out
+    double explore_eps = 0.0;       // probability of taking the other action (training data)
+    std::mt19937_64 explore_rng{0};
+    // learned-schedule state
+    int passes_at_level = 0;
+    double prev_miss = 1.0;
+    uint64_t level_start_V = 0, prev_level_start_V = 0;
     // state
     bool begun = false;
     bool heads_dirty = false;  // a round stopped before its commit cleared the candidate lists
@@ -250,6 +269,8 @@ struct rsagpu_algo {
         dfree(block_offsets);
         dfree(d_err);
         dfree(d_visits);
+        dfree(d_mlp);
+        dfree(d_feat);
         if (h_counters) cudaFreeHost(h_counters);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
@@ -412,7 +433,9 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
     }
     a.phase = dalloc<int32_t>(ncells);
     G.head = dalloc<int32_t>(ncells);
+    G.cocc = dalloc<uint32_t>(nwords);
     CK(cudaMemset(a.occ, 0, nwords * sizeof(uint32_t)));
+    CK(cudaMemset(G.cocc, 0, nwords * sizeof(uint32_t)));
     CK(cudaMemset(G.head, 0xFF, ncells * sizeof(int32_t)));
     G.ready = true;
 }
@@ -453,6 +476,7 @@ CandArgs cand_args(rsagpu_algo* A, uint32_t n) {
     CandArgs c = A->cand.a;
     c.n = n;
     c.head = A->dom->grid.head;
+    c.cocc = A->dom->grid.cocc;
     c.und = c.counters + COUNTERS;
     return c;
 }
@@ -508,6 +532,10 @@ void begin(rsagpu_algo* A) {
     A->stats.peak_voxels = V;
     A->mask_ms.clear();
     A->mask_bytes.clear();
+    A->passes_at_level = 0;
+    A->prev_miss = 1.0;
+    A->level_start_V = V;
+    A->prev_level_start_V = 0;
 }
 
 // remove_covered + subdivide_uncovered (list_of_voxels.ixx:30-100)
@@ -639,12 +667,14 @@ float ev_ms(rsagpu_algo* A, int a, int b) {
 
 // One round on candidates already in the buffers (state = UNDECIDED): probe, settle, cap, commit.
 // Returns the number accepted.
-uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_outreach, bool keep_state) {
+uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_outreach, bool keep_state,
+                      uint64_t* n_greedy = nullptr) {
     rsagpu_domain* dom = A->dom;
     const GridArgs& g = dom->grid.a;
     if (A->heads_dirty) {
         // stale list heads would link this round's candidates to indices of an unfinished round
         CK(cudaMemsetAsync(dom->grid.head, 0xFF, g.ncells * sizeof(int32_t), A->stream));
+        CK(cudaMemsetAsync(dom->grid.cocc, 0, ((g.ncells + 31) / 32 + 1) * sizeof(uint32_t), A->stream));
         A->heads_dirty = false;
     }
     A->heads_dirty = true;
@@ -683,11 +713,13 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
     while (used < it && A->h_counters[COUNTERS + used] != 0) used++;
     A->stats.settle_iterations += used;
     ev_record(A, 4);
+    uint64_t greedy = 0;
     if (may_outreach) {
         ops->gather_accepted(c, A->stream);
         CK(cudaMemcpyAsync(A->h_counters + 3, c.counters + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
         CK(cudaStreamSynchronize(A->stream));
         const uint64_t nacc = A->h_counters[3];
+        greedy = nacc;
         if (nacc > max_new) {
             std::vector<uint64_t> keys(nacc);
             CK(cudaMemcpyAsync(keys.data(), c.gather, nacc * sizeof(uint64_t), cudaMemcpyDeviceToHost, A->stream));
@@ -718,6 +750,7 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
     CK(cudaMemcpyAsync(A->h_counters, c.counters, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaStreamSynchronize(A->stream));
     A->stats.retests += A->h_counters[4];
+    if (n_greedy) *n_greedy = may_outreach ? greedy : A->h_counters[1];
     if (A->h_counters[2] & ERR_DOUBLE_OCCUPANCY)
         raise(RSAGPU_ERR_INVARIANT, "two accepted centres in one grid cell");
     (void)keep_state;
@@ -732,16 +765,66 @@ void reset_counters(rsagpu_algo* A) {
 
 // RadiusGenerator::update_placed (radius_generator.ixx:62-68) + the miss-rate rule (operator_algorithm.ixx:
 // 140-162, 190-206).  Returns true when no class is left.
-bool end_round(rsagpu_algo* A, uint64_t n_shots, uint64_t n_new, bool* refined, double thr) {
+int mlp_decide_host(rsagpu_algo* A, const float* feat, bool* refine);
+
+bool end_round(rsagpu_algo* A, uint64_t n_shots, uint64_t n_new, bool* refined, double thr, uint64_t n_hits,
+               TraceRow* row = nullptr) {
     rsagpu_radgen& rg = A->rg;
     if (rg.idx < (int)rg.n.size()) {
         rg.n[rg.idx] = rg.n[rg.idx] - n_new;
         if (rg.n[rg.idx] == 0) rg.idx++;
     }
     const bool done = rg.idx >= (int)rg.n.size();
-    const double miss = (double)(n_shots - n_new) / (0.000001 + (double)n_shots);
+    const double miss = (double)(n_shots - n_hits) / (0.000001 + (double)n_shots);
     *refined = false;
-    if (miss > thr) {
+    bool do_refine = miss > thr;
+    if (row) {
+        // state features of the learned schedule (documented in rsa_mpi_gb300/schedule.py)
+        const int D = A->dom->dim;
+        const GridArgs& g = A->dom->grid.a;
+        double vol = 1;
+        for (int d = 0; d < D; d++) vol *= A->dom->L[d];
+        const double r = A->rg.r[std::min<int>(rg.idx, (int)rg.r.size() - 1)];
+        uint64_t V0 = 1;
+        for (int d = 0; d < D; d++) V0 *= (uint64_t)A->nvox0[d];
+        float* f = row->features;
+        f[0] = (float)(std::log2((double)A->V + 1) / 32);
+        f[1] = (float)A->level / 32;
+        f[2] = (float)miss;
+        f[3] = (float)(A->passes_at_level > 0 ? A->prev_miss : miss);
+        f[4] = (float)std::min(A->passes_at_level, 16) / 16;
+        f[5] = (float)(std::log2((double)n_shots + 1) / 32);
+        f[6] = (float)(std::log2((double)n_hits + 1) / 32);
+        f[7] = (float)(std::log2((double)A->placed + 1) / 32);
+        f[8] = (float)(A->placed * ball_volume(D, r) / vol);
+        f[9] = (float)D / 8;
+        f[10] = (float)(std::log2((double)A->V / (double)g.ncells + 1e-9) / 32);
+        f[11] = (float)((double)n_hits / ((double)A->V + 1));
+        f[12] = (float)(std::log2((double)V0) / 32);
+        f[13] = (float)(A->prev_level_start_V > 0
+                            ? (double)A->level_start_V / ((double)A->prev_level_start_V * (double)(1u << D))
+                            : 1.0);
+        f[14] = miss > thr ? 1.f : 0.f;
+        f[15] = 1.f;
+        if (A->schedule == RSAGPU_SCHEDULE_LEARNED && !A->mlp.empty()) {
+            bool r_mlp = do_refine;
+            if (mlp_decide_host(A, f, &r_mlp) == RSAGPU_OK) do_refine = r_mlp;  // else: heuristic fallback
+        }
+        if (A->explore_eps > 0) {
+            std::uniform_real_distribution<double> U(0, 1);
+            if (U(A->explore_rng) < A->explore_eps) do_refine = !do_refine;
+        }
+        if (A->schedule == RSAGPU_SCHEDULE_LEARNED || A->explore_eps > 0) {
+            // guard rails neither the network nor exploration may cross: subdividing while more than a tenth
+            // of the darts still land multiplies the voxels by nearly 2^D per level (little of them is
+            // covered yet); a pass that places nothing must subdivide (or nothing changes)
+            if (miss < 0.9) do_refine = false;
+            if (miss > 0.999 || A->passes_at_level >= 32) do_refine = true;
+        }
+        A->prev_miss = miss;
+        A->passes_at_level++;
+    }
+    if (do_refine && A->V > 0) {
         ev_record(A, 6);
         refine(A);
         ev_record(A, 7);
@@ -750,8 +833,28 @@ bool end_round(rsagpu_algo* A, uint64_t n_shots, uint64_t n_new, bool* refined, 
             A->stats.ms_refine += ev_ms(A, 6, 7);
         }
         *refined = true;
+        A->prev_level_start_V = A->level_start_V;
+        A->level_start_V = A->V;
+        A->passes_at_level = 0;
     }
     return done;
+}
+
+int mlp_decide_host(rsagpu_algo* A, const float* feat, bool* refine) {
+    if (!A->d_mlp) {
+        A->d_mlp = (uint16_t*)dalloc<uint16_t>(A->mlp.size());
+        A->d_feat = dalloc<float>(NFEAT + 2);
+        CK(cudaMemcpy(A->d_mlp, A->mlp.data(), A->mlp.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpyAsync(A->d_feat, feat, NFEAT * sizeof(float), cudaMemcpyHostToDevice, A->stream));
+    const int rc = mlp_decide(A->d_mlp, A->d_feat, A->d_feat + NFEAT, A->stream);
+    if (rc != RSAGPU_OK) return rc;
+    float y[2];
+    CK(cudaMemcpyAsync(y, A->d_feat + NFEAT, 2 * sizeof(float), cudaMemcpyDeviceToHost, A->stream));
+    CK(cudaStreamSynchronize(A->stream));
+    if (!std::isfinite(y[0]) || !std::isfinite(y[1])) return RSAGPU_ERR_STATE;
+    *refine = y[1] < y[0];  // smaller predicted remaining time
+    return RSAGPU_OK;
 }
 
 double threshold(const rsagpu_algo* A) {
@@ -792,6 +895,11 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         if (A->rg.idx >= (int)A->rg.n.size()) break;
         const uint64_t remaining = A->rg.n[A->rg.idx];
         uint64_t C = darts_for(A);
+        if (A->schedule != RSAGPU_SCHEDULE_REFERENCE) {
+            // no more than 16x the spheres still wanted of this class
+            const double cap = std::max(16.0 * (double)remaining, (double)A->min_darts);
+            if ((double)C > cap) C = (uint64_t)cap;
+        }
         const bool may = C >= remaining;
         ensure_cand(A, C);
         reset_counters(A);
@@ -804,15 +912,28 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         da.round = A->round++;
         da.radius = A->rg.r[A->rg.idx];
         da.phase = A->rg.phase[A->rg.idx];
+        const auto tp0 = std::chrono::steady_clock::now();
         ev_record(A, 0);
         CandArgs c = cand_args(A, (uint32_t)C);
         A->ops->darts(dom->grid.a, c, da, A->stream);
         ev_record(A, 1);
-        const uint64_t n_new = decide_round(A, (uint32_t)C, remaining, may, false);
+        uint64_t n_hits = 0;
+        const uint64_t n_new = decide_round(A, (uint32_t)C, remaining, may, false, &n_hits);
         if (A->timing) A->stats.ms_darts += ev_ms(A, 0, 1);
-        TraceRow row{A->V, C, n_new, 0, A->level};
+        TraceRow row{};
+        row.voxels = A->V;
+        row.darts = C;
+        row.accepted = n_new;
+        row.level = A->level;
+        const auto tp1 = std::chrono::steady_clock::now();
         bool refined = false;
-        const bool done = end_round(A, C, n_new, &refined, thr);
+        // the miss rate of the geometry: darts the count cap dropped are not misses (with 10^7-dart rounds the
+        // cap would otherwise read as a miss rate near 1 and refine every round)
+        const bool done = end_round(A, C, n_new, &refined, thr, n_hits, &row);
+        CK(cudaStreamSynchronize(A->stream));
+        const auto tp2 = std::chrono::steady_clock::now();
+        row.pass_ms = std::chrono::duration<double, std::milli>(tp1 - tp0).count();
+        row.refine_ms = std::chrono::duration<double, std::milli>(tp2 - tp1).count();
         row.refined = refined;
         A->trace.push_back(row);
         A->stats.rounds++;
@@ -1137,6 +1258,8 @@ int rsagpu_algo_set_mlp(rsagpu_algo* algo, const uint16_t* w, uint64_t n) {
         if (!algo || !w) raise(RSAGPU_ERR_ARG, "null argument");
         if (n != 5378) raise(RSAGPU_ERR_ARG, "expected 5378 weights, got %llu", (unsigned long long)n);
         algo->mlp.assign(w, w + n);
+        dfree(algo->d_mlp);
+        dfree(algo->d_feat);
     });
 }
 
@@ -1146,6 +1269,29 @@ int rsagpu_algo_kernel_profile(rsagpu_algo* algo, double* ms, double* bytes, uin
     for (uint64_t i = 0; i < std::min<uint64_t>(cap, algo->mask_ms.size()); i++) {
         if (ms) ms[i] = algo->mask_ms[i];
         if (bytes) bytes[i] = algo->mask_bytes[i];
+    }
+    return RSAGPU_OK;
+}
+
+int rsagpu_algo_set_exploration(rsagpu_algo* algo, double epsilon, uint64_t seed) {
+    if (!algo || !(epsilon >= 0 && epsilon <= 1)) return fail(RSAGPU_ERR_ARG, "invalid exploration");
+    algo->explore_eps = epsilon;
+    algo->explore_rng.seed(seed);
+    return RSAGPU_OK;
+}
+
+int rsagpu_algo_trace_features(rsagpu_algo* algo, float* features, uint8_t* refined, double* pass_ms,
+                               double* refine_ms, uint64_t cap, uint64_t* n_out) {
+    if (!algo || !n_out) return fail(RSAGPU_ERR_ARG, "null argument");
+    *n_out = algo->trace.size();
+    const uint64_t n = std::min<uint64_t>(cap, algo->trace.size());
+    for (uint64_t i = 0; i < n; i++) {
+        const TraceRow& t = algo->trace[i];
+        if (features)
+            for (int k = 0; k < NFEAT; k++) features[i * NFEAT + k] = t.features[k];
+        if (refined) refined[i] = t.refined;
+        if (pass_ms) pass_ms[i] = t.pass_ms;
+        if (refine_ms) refine_ms[i] = t.refine_ms;
     }
     return RSAGPU_OK;
 }
@@ -1246,7 +1392,7 @@ int rsagpu_algo_end_round(rsagpu_algo* algo, uint64_t n_shots, uint64_t n_new, i
         if (!algo->begun) raise(RSAGPU_ERR_STATE, "end_round before begin");
         set_device(algo->dom);
         bool r = false;
-        const bool dn = end_round(algo, n_shots, n_new, &r, reference_miss_threshold(algo->dom->dim));
+        const bool dn = end_round(algo, n_shots, n_new, &r, reference_miss_threshold(algo->dom->dim), n_new);
         CK(cudaStreamSynchronize(algo->stream));
         if (refined) *refined = r;
         if (done) *done = dn;
@@ -1317,17 +1463,6 @@ int rsagpu_batch_run(const rsagpu_instance_desc* inst, int n, uint64_t* counts_o
                      double* seconds_out) {
     return fail(RSAGPU_ERR_STATE, "batch form not built yet (%p %d %p %p %p)", (const void*)inst, n, (void*)counts_out,
                 (void*)fractions_out, (void*)seconds_out);
-}
-
-int rsagpu_mlp_forward(const uint16_t* w, const float* x, uint64_t n, float* y) {
-    return fail(RSAGPU_ERR_STATE, "mlp not built yet (%p %p %llu %p)", (const void*)w, (const void*)x,
-                (unsigned long long)n, (void*)y);
-}
-
-int rsagpu_mlp_train_step(float* master, uint16_t* w, const float* x, const float* t, uint64_t n, float lr,
-                          float* loss, float* grad) {
-    return fail(RSAGPU_ERR_STATE, "mlp not built yet (%p %p %p %p %llu %f %p %p)", (void*)master, (void*)w,
-                (const void*)x, (const void*)t, (unsigned long long)n, lr, (void*)loss, (void*)grad);
 }
 
 }  // extern "C"

@@ -144,7 +144,7 @@ class Algo:
     def set_cap_rule(self, rule: int):
         check(lib().rsagpu_algo_set_cap_rule(self._h, rule))
 
-    def set_schedule(self, factor=1.0, min_darts=4096, max_darts=1 << 25, miss_threshold=-1.0):
+    def set_schedule(self, factor=0.25, min_darts=4096, max_darts=1 << 26, miss_threshold=0.99):
         check(lib().rsagpu_algo_set_schedule_params(self._h, float(factor), int(min_darts), int(max_darts),
                                                     float(miss_threshold)))
 
