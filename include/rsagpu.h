@@ -170,17 +170,36 @@ int rsagpu_algo_voxels(rsagpu_algo* algo, int64_t* coords, uint64_t cap, uint64_
 int rsagpu_algo_draw_darts(rsagpu_algo* algo, uint64_t seed, uint64_t round, uint64_t n,
                            double* pos, uint64_t* key, uint64_t* voxel_index);
 
-/* ---- batch: many independent instances in one persistent launch sequence. */
+/* ---- batched instances ----
+ * No counterpart in the reference, which runs one domain per process (rsa_algo::proceed_voxel,
+ * operator_algorithm.ixx:85-188).  Runs n independent one-radius instances to certified maximality:
+ * instance i is the box [0, sup[0..dim-1]] with spheres of one radius and the Philox key seed.  It places
+ * exactly the spheres of its own single-instance run: rsagpu_domain_create([0], sup, radius),
+ * rsagpu_radgen_create_fractions({radius}, {1.0}, {0}, 1, box volume, 0), rsagpu_algo_create(.., 6000),
+ * rsagpu_algo_set_form(form, RSAGPU_SCHEDULE_HEURISTIC) with the default schedule, rsagpu_algo_proceed(seed).
+ * The instances of one dimension advance together, one launch sequence per round over every unfinished
+ * instance, in waves whose estimated device memory fits max_bytes (0 = 60% of the free memory).  With
+ * autotune != 0 the block shapes of the probe, collect, settle and voxel-mask kernels are chosen by timing
+ * (outputs never depend on them).  Outputs per instance (each pointer may be NULL): counts_out = spheres;
+ * checksums_out = sum mod 2^64 over its spheres of h, where h starts at 0x9E3779B97F4A7C15 and for each
+ * coordinate x_d in order becomes mix64(h ^ bits(x_d)) (mix64 = splitmix64's output function:
+ * z ^= z >> 30; z *= 0xbf58476d1ce4e5b9; z ^= z >> 27; z *= 0x94d049bb133111eb; z ^= z >> 31);
+ * seconds_out = time from the call's start until the instance was certified maximal. */
 typedef struct {
     int dim;
     double sup[RSAGPU_MAX_DIM];  /* box [0, sup] */
-    double radius;               /* monodisperse radius */
-    uint64_t seed;
+    double radius;               /* the one radius */
+    uint64_t seed;               /* Philox key of the instance's darts */
 } rsagpu_instance_desc;
-/* Runs every instance to certified maximality; counts_out[i] = spheres of instance i.
- * fractions_out (may be NULL) = packing fraction of each instance. */
-int rsagpu_batch_run(const rsagpu_instance_desc* inst, int n, uint64_t* counts_out,
-                     double* fractions_out, double* seconds_out);
+typedef struct {
+    double seconds;              /* wall time of the call */
+    uint64_t waves, rounds, darts, retests, peak_voxels, launches, budget_bytes;
+    int32_t block[RSAGPU_MAX_DIM + 1][4]; /* threads per block chosen per dimension for probe, collect,
+                                             settle, voxel mask (0 = not tuned) */
+} rsagpu_batch_stats;
+int rsagpu_batch_run(const rsagpu_instance_desc* inst, int n, int form, uint64_t max_bytes, int autotune,
+                     uint64_t* counts_out, uint64_t* checksums_out, double* seconds_out,
+                     rsagpu_batch_stats* stats_out);
 
 /* ---- learned schedule: MLP kernels (16-64-64-2, bf16 weights, fp32 accumulate) ---- */
 /* forward: x[n][16] (fp32) -> y[n][2] (fp32), weights as rsagpu_algo_set_mlp */

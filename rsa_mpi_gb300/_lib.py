@@ -57,6 +57,12 @@ class InstanceDesc(C.Structure):
     _fields_ = [("dim", C.c_int), ("sup", C.c_double * MAX_DIM), ("radius", C.c_double), ("seed", C.c_uint64)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("seconds", C.c_double)] + [(n, C.c_uint64) for n in (
+        "waves", "rounds", "darts", "retests", "peak_voxels", "launches", "budget_bytes")] + \
+        [("block", (C.c_int32 * 4) * (MAX_DIM + 1))]
+
+
 _lib = None
 
 _SIGS = {
@@ -96,7 +102,8 @@ _SIGS = {
     "rsagpu_algo_refine": (C.c_int, [_vp]),
     "rsagpu_algo_voxels": (C.c_int, [_vp, _i64, C.c_uint64, _u64, C.POINTER(C.c_int32), _d]),
     "rsagpu_algo_draw_darts": (C.c_int, [_vp, C.c_uint64, C.c_uint64, C.c_uint64, _d, _u64, _u64]),
-    "rsagpu_batch_run": (C.c_int, [C.POINTER(InstanceDesc), C.c_int, _u64, _d, _d]),
+    "rsagpu_batch_run": (C.c_int, [C.POINTER(InstanceDesc), C.c_int, C.c_int, C.c_uint64, C.c_int, _u64, _u64, _d,
+                                   C.POINTER(BatchStats)]),
     "rsagpu_mlp_forward": (C.c_int, [_u16, _f32, C.c_uint64, _f32]),
     "rsagpu_resolve_batch_noalloc": (C.c_int, [C.c_int, _d, _d, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_uint64, C.c_void_p, C.c_void_p]),

@@ -49,7 +49,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for d in DIMS:
         jobs.append(([nvcc(), *ARCH, *FLAGS, f"-DRSA_DIM={d}", "-c", os.path.join(CSRC, "kernels.cu"),
                       "-o", os.path.join(OUT, f"kernels_d{d}.o")], f"kernels_d{d}"))
-    for name in ("kernels_common", "rsagpu", "noalloc", "mlp"):
+    for name in ("kernels_common", "rsagpu", "batch", "noalloc", "mlp"):
         jobs.append(([nvcc(), *ARCH, *FLAGS, "-c", os.path.join(CSRC, f"{name}.cu"),
                       "-o", os.path.join(OUT, f"{name}.o")], name))
 
@@ -65,7 +65,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         list(ex.map(run, jobs))
     objs = [os.path.join(OUT, f"kernels_d{d}.o") for d in DIMS]
-    objs += [os.path.join(OUT, f"{n}.o") for n in ("kernels_common", "rsagpu", "noalloc", "mlp")]
+    objs += [os.path.join(OUT, f"{n}.o") for n in ("kernels_common", "rsagpu", "batch", "noalloc", "mlp")]
     tmp = LIB + ".tmp"
     r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"], capture_output=True, text=True)
     if r.returncode != 0:

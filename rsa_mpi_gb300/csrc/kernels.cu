@@ -5,6 +5,7 @@
 // and one refinement (update_covered_voxels, :190-206) is
 //   k_refine_mask -> scan of block counts -> k_refine_write.
 #include <cfloat>
+#include <vector>
 
 #include "rsa_device.cuh"
 #include "rsa_ops.h"
@@ -118,9 +119,8 @@ struct DartParams {
     uint64_t* vidx_out;
 };
 
-__global__ void k_darts(DartParams p) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+// Dart i of the round (counter (i, round, call) under the run's key), written to candidate slot o.
+__device__ __forceinline__ void dart_body(const DartParams& p, uint32_t i, uint64_t o) {
     constexpr int WORDS = 2 + 2 * D + 1;
     constexpr int CALLS = (WORDS + 3) / 4;
     uint32_t w[CALLS * 4];
@@ -135,18 +135,24 @@ __global__ void k_darts(DartParams p) {
     }
     const uint64_t r64 = ((uint64_t)w[0] << 32) | w[1];
     const uint64_t v = __umul64hi(r64, p.V);
-    if (p.vidx_out) p.vidx_out[i] = v;
+    if (p.vidx_out) p.vidx_out[o] = v;
 #pragma unroll
     for (int d = 0; d < D; d++) {
         const uint64_t bits = (((uint64_t)w[2 + 2 * d] << 32) | w[3 + 2 * d]) >> 11;  // 53 bits
         const double u = (double)bits * 0x1.0p-53;
         const double orig = __dadd_rn(p.inf[d], __dmul_rn((double)p.vox[v * D + d], p.len[d]));
-        p.pos[(uint64_t)i * D + d] = __dadd_rn(orig, __dmul_rn(p.len[d], u));
+        p.pos[o * D + d] = __dadd_rn(orig, __dmul_rn(p.len[d], u));
     }
-    p.key[i] = ((uint64_t)w[2 + 2 * D] << 32) | i;
-    p.rad[i] = p.radius;
-    p.cphase[i] = p.phase;
-    p.state[i] = ST_UNDECIDED;
+    p.key[o] = ((uint64_t)w[2 + 2 * D] << 32) | i;
+    p.rad[o] = p.radius;
+    p.cphase[o] = p.phase;
+    p.state[o] = ST_UNDECIDED;
+}
+
+__global__ void k_darts(DartParams p) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    dart_body(p, i, i);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -154,12 +160,11 @@ __global__ void k_darts(DartParams p) {
 // (remove_collisions_with_validated_spheres, operator_cells_and_data_storage.ixx:54-76); the
 // others are linked into the candidate cell lists and appended to the alive list.
 // ------------------------------------------------------------------------------------------------
+// Probe of undecided candidate i; returns true when it stays alive (linked into the cell lists).
 template <bool F32>
-__global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool alive = false;
-    uint32_t rt = 0;
-    if (i < c.n && c.state[i] == ST_UNDECIDED) {
+__device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, uint32_t i,
+                                           uint32_t& rt) {
+    {
         double x[D];
 #pragma unroll
         for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
@@ -201,14 +206,21 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
         }
         if (hit) {
             c.state[i] = ST_DEAD;
-        } else {
-            const int64_t idx = cell_index<D>(g, k);
-            c.cell[i] = idx;
-            c.next[i] = atomicExch(c.head + idx, (int32_t)i);
-            atomicOr(c.cocc + (idx >> 5), 1u << (idx & 31));
-            alive = true;
+            return false;
         }
+        const int64_t idx = cell_index<D>(g, k);
+        c.cell[i] = idx;
+        c.next[i] = atomicExch(c.head + idx, (int32_t)i);
+        atomicOr(c.cocc + (idx >> 5), 1u << (idx & 31));
+        return true;
     }
+}
+
+template <bool F32>
+__global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t rt = 0;
+    const bool alive = i < c.n && c.state[i] == ST_UNDECIDED && probe_body<F32>(g, geo, c, i, rt);
     const uint32_t slot = warp_append(&c.counters[0], alive);
     if (alive) c.alive[slot] = i;
     if (F32) {
@@ -305,14 +317,11 @@ __device__ __forceinline__ uint8_t load_state(const uint8_t* s, int32_t j) {
 // candidate whose blockers are all rejected and reject one with an accepted blocker.  The smallest
 // undecided key always settles, so each iteration makes progress.
 // ------------------------------------------------------------------------------------------------
+// Collects the overlapping candidates that precede alive candidate i; returns true when it stays undecided.
 template <bool F32>
-__global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nalive = c.counters[0];
-    bool undecided = false;
-    uint32_t rt = 0;
-    if (t < nalive) {
-        const uint32_t i = c.alive[t];
+__device__ __forceinline__ bool collect_body(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, uint32_t i,
+                                             uint32_t& rt) {
+    {
         double x[D];
 #pragma unroll
         for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
@@ -348,11 +357,19 @@ __global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
         }
         if (nb == 0) {
             c.state[i] = ST_ACCEPTED;
-        } else {
-            c.nblk[i] = nb > NB ? (uint8_t)NB_OVERFLOW : (uint8_t)nb;
-            undecided = true;
+            return false;
         }
+        c.nblk[i] = nb > NB ? (uint8_t)NB_OVERFLOW : (uint8_t)nb;
+        return true;
     }
+}
+
+template <bool F32>
+__global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    uint32_t rt = 0;
+    const bool undecided = t < nalive && collect_body<F32>(g, geo, c, c.alive[t], rt);
     const uint32_t mask = __ballot_sync(0xffffffffu, undecided);
     if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[0], (uint32_t)__popc(mask));
     if (F32) {
@@ -362,19 +379,13 @@ __global__ void k_collect(Grid<D> g, Geo<D> geo, CandArgs c) {
     }
 }
 
+// One settle step of alive candidate i; returns true when it is still undecided.
 template <bool F32>
-__global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
-    if (c.und[it - 1] == 0) return;
-    const uint32_t nalive = c.counters[0];
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t rounds = (nalive + stride - 1) / stride;  // same trip count for every lane
-    uint32_t rt = 0;
-    for (uint32_t rr = 0; rr < rounds; rr++) {
-        const uint32_t t = t0 + rr * stride;
-        bool still = false;
-        if (t < nalive) {
-            const uint32_t i = c.alive[t];
+__device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, uint32_t i,
+                                            uint32_t& rt) {
+    bool still = false;
+    {
+        {
             if (load_state(c.state, i) == ST_UNDECIDED) {
                 bool any_acc = false, all_rej = true;
                 const uint8_t nb = c.nblk[i];
@@ -420,6 +431,21 @@ __global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
                 else still = true;
             }
         }
+    }
+    return still;
+}
+
+template <bool F32>
+__global__ void k_settle(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
+    if (c.und[it - 1] == 0) return;
+    const uint32_t nalive = c.counters[0];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t rounds = (nalive + stride - 1) / stride;  // same trip count for every lane
+    uint32_t rt = 0;
+    for (uint32_t rr = 0; rr < rounds; rr++) {
+        const uint32_t t = t0 + rr * stride;
+        const bool still = t < nalive && settle_body<F32>(g, geo, c, c.alive[t], rt);
         const uint32_t mask = __ballot_sync(0xffffffffu, still);
         if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[it], (uint32_t)__popc(mask));
     }
@@ -458,12 +484,10 @@ __global__ void k_cut_accepted(CandArgs c, int use_pivot, double pivot, uint64_t
 }
 
 // commit: accepted candidates become placed spheres; the candidate lists are cleared.
-__global__ void k_commit(Grid<D> g, Geo<D> geo, CandArgs c) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nalive = c.counters[0];
+// Commit of alive candidate i; returns true when it was accepted (and is now a placed sphere).
+__device__ __forceinline__ bool commit_body(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, uint32_t i) {
     bool acc = false;
-    if (t < nalive) {
-        const uint32_t i = c.alive[t];
+    {
         const int64_t idx = c.cell[i];
         c.head[idx] = -1;
         atomicAnd(c.cocc + (idx >> 5), ~(1u << (idx & 31)));
@@ -481,13 +505,21 @@ __global__ void k_commit(Grid<D> g, Geo<D> geo, CandArgs c) {
                 g.pos[idx * D + d] = x;
                 // FP32 screening offset from the cell's corner (guard-band form)
                 const double base = __dadd_rn(geo.inf[d], __dmul_rn((double)kd, g.c[d]));
-                ((float*)g.off)[idx * D + d] = __double2float_rn(__dsub_rn(x, base));
+                if (g.off) ((float*)g.off)[idx * D + d] = __double2float_rn(__dsub_rn(x, base));
             }
-            g.rad[idx] = c.rad[i];
-            ((float*)g.radf)[idx] = __double2float_rn(c.rad[i]);
-            g.phase[idx] = c.phase[i];
+            // a one-radius grid without per-cell radius or phase arrays (batched instances) skips them
+            if (g.rad) g.rad[idx] = c.rad[i];
+            if (g.radf) ((float*)g.radf)[idx] = __double2float_rn(c.rad[i]);
+            if (g.phase) g.phase[idx] = c.phase[i];
         }
     }
+    return acc;
+}
+
+__global__ void k_commit(Grid<D> g, Geo<D> geo, CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    const bool acc = t < nalive && commit_body(g, geo, c, c.alive[t]);
     const uint32_t mask = __ballot_sync(0xffffffffu, acc);
     if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.counters[1], (uint32_t)__popc(mask));
 }
@@ -578,19 +610,15 @@ __device__ __forceinline__ void children_covered_wide(const double* dl0, const d
 
 constexpr uint64_t FAR_MARGIN_ULPS = 1ull << 13;  // relative 2^-39, far above the rounding of a distance
 
-__global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> geo, RefineParams p) {
-    const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
-    uint32_t mask[MASK_WORDS];
-#pragma unroll
-    for (int w = 0; w < MASK_WORDS; w++) mask[w] = 0;
+// Child mask of the parent voxel with coordinates cc (mask[] zeroed by the caller); returns true when
+// remove_covered keeps the parent.
+__device__ __forceinline__ bool refine_mask64_body(const Grid<D>& g, const Geo<D>& geo, const RefineParams& p,
+                                                   const int64_t* cc, uint32_t* mask, uint32_t& visits) {
     bool survived = false;
-    uint32_t visits = 0;
-    if (v < p.V) {
-        int64_t cc[D];
+    {
         double orig[D], centre[D];
 #pragma unroll
         for (int d = 0; d < D; d++) {
-            cc[d] = p.vin[v * D + d];
             orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cc[d], p.len[d]));
             // center(i) = origin + (coord + 0.5) * len (list_of_voxels.ixx:154-160)
             centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cc[d], 0.5), p.len[d]));
@@ -681,6 +709,22 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
                 mask[w] = ~cov[w] & all;
             }
         }
+    }
+    return survived;
+}
+
+__global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> geo, RefineParams p) {
+    const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
+    uint32_t mask[MASK_WORDS];
+#pragma unroll
+    for (int w = 0; w < MASK_WORDS; w++) mask[w] = 0;
+    bool survived = false;
+    uint32_t visits = 0;
+    if (v < p.V) {
+        int64_t cc[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) cc[d] = p.vin[v * D + d];
+        survived = refine_mask64_body(g, geo, p, cc, mask, visits);
 #pragma unroll
         for (int w = 0; w < MASK_WORDS; w++) p.masks[v * MASK_WORDS + w] = mask[w];
     }
@@ -706,21 +750,15 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
 // origin, centre and their offsets from the centre's cell corner are computed in FP64 (O(D) work);
 // each (voxel, sphere) test is FP32 unless it falls inside the guard band, where it is redone in FP64
 // exactly as the FP64 kernel does.
-__global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask32(Grid<D> g, Geo<D> geo, RefineParams p) {
-    const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
-    uint32_t mask[MASK_WORDS];
-#pragma unroll
-    for (int w = 0; w < MASK_WORDS; w++) mask[w] = 0;
+__device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D>& geo, const RefineParams& p,
+                                                   const int64_t* cc, uint32_t* mask, uint32_t& visits, uint32_t& rt) {
     bool survived = false;
-    uint32_t visits = 0, rt = 0;
-    if (v < p.V) {
-        int64_t cc[D];
+    {
         double orig[D], centre[D];
         float relo[D], relc[D];
         int32_t k[D];
 #pragma unroll
         for (int d = 0; d < D; d++) {
-            cc[d] = p.vin[v * D + d];
             orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cc[d], p.len[d]));
             centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cc[d], 0.5), p.len[d]));
         }
@@ -883,6 +921,22 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask32(Grid<D> g, Geo<D
                 mask[w] = ~cov[w] & all;
             }
         }
+    }
+    return survived;
+}
+
+__global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask32(Grid<D> g, Geo<D> geo, RefineParams p) {
+    const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
+    uint32_t mask[MASK_WORDS];
+#pragma unroll
+    for (int w = 0; w < MASK_WORDS; w++) mask[w] = 0;
+    bool survived = false;
+    uint32_t visits = 0, rt = 0;
+    if (v < p.V) {
+        int64_t cc[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) cc[d] = p.vin[v * D + d];
+        survived = refine_mask32_body(g, geo, p, cc, mask, visits, rt);
 #pragma unroll
         for (int w = 0; w < MASK_WORDS; w++) p.masks[v * MASK_WORDS + w] = mask[w];
     }
@@ -1150,6 +1204,8 @@ void op_extract_write(const GridArgs& ga, const uint64_t* block_offsets, double*
     count_launch();
 }
 
+#include "kernels_batch.cuh"
+
 const DimOps kOps = {
     D,
     op_vox_init,
@@ -1167,6 +1223,18 @@ const DimOps kOps = {
     op_extract_write,
     CHILDREN,
     MASK_WORDS,
+    op_batch_table_bytes,
+    op_batch_table_fill,
+    op_b_vox_init,
+    op_b_darts,
+    op_b_probe,
+    op_b_collect,
+    op_b_settle,
+    op_b_commit,
+    op_b_refine_mask,
+    op_b_refine_offsets,
+    op_b_refine_write,
+    op_b_results,
 };
 
 }  // namespace

@@ -239,7 +239,7 @@ __device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo
 #pragma unroll
                 for (int d = 0; d < D; d++) p[d] = g.pos[idx * D + d];
                 image_of<D>(geo, p, q, img);
-                if (f(idx, img, g.rad[idx])) return true;
+                if (f(idx, img, g.mono ? g.rmono : g.rad[idx])) return true;
             }
         }
         return false;

@@ -84,6 +84,45 @@ struct RefineArgs {
     unsigned long long* retests; // (voxel, sphere) pairs redone in FP64 (guard-band form)
 };
 
+// ------------------------------------------------------------------------------------------------
+// batched instances: many independent one-radius instances of one dimension share every launch.
+// Each instance owns a segment of the wave's arrays (cells, voxels, darts); a thread finds the
+// instance of its element by binary search over the segment offsets.
+// ------------------------------------------------------------------------------------------------
+struct BatchInstance {   // host description of one instance of a wave
+    GridArgs g;          // its grid (mono = 1); pointers into the wave's arrays
+    int32_t* head;       // its candidate lists and candidate occupancy bits
+    uint32_t* cocc;
+    uint64_t seed;       // Philox key of its darts
+    int64_t nvox0[MAX_D];  // level-0 voxels per dimension
+};
+
+struct BatchRound {      // per instance, per round
+    uint64_t vbase;      // first voxel of its segment
+    uint64_t V;          // voxels in its segment
+    double len[MAX_D];   // voxel length at its level
+    double nlen[MAX_D];  // child length = 0.5 * len
+    int32_t refine;      // subdivide its voxels after this round's pass
+};
+
+struct BatchArgs {
+    uint32_t M;                // instances in the wave
+    const void* table;         // per-dimension instance table (DimOps::batch_table_fill)
+    const BatchRound* rnd;     // M entries
+    const uint64_t* dart_off;  // M + 1: the darts of instance s are [dart_off[s], dart_off[s + 1])
+    const uint64_t* vox_off;   // M + 1: its voxels
+    const uint64_t* word_off;  // M + 1: its occupancy words (32 cells each)
+    const int64_t* vox;        // the wave's voxel list (D coordinates per voxel)
+    uint32_t* cinst;           // instance of each candidate
+    uint32_t* acc;             // spheres accepted per instance in the current round
+    uint64_t round;            // round index (the Philox counter's round words)
+    uint64_t ndarts;           // darts of the round, all instances
+    uint64_t V;                // voxels, all instances
+    uint64_t nwords;           // occupancy words, all instances
+    const uint32_t* occ;       // the wave's occupancy bits and centres (results pass)
+    const double* pos;
+};
+
 struct DimOps {
     int D;
     void (*vox_init)(int64_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s);
@@ -102,6 +141,20 @@ struct DimOps {
                           int32_t* phase, cudaStream_t s);
     int children;      // 2^D
     int mask_words;    // 32-bit words of child mask per voxel
+    // batched instances (block = threads per block, from the autotuner)
+    uint64_t (*batch_table_bytes)(uint32_t M);
+    // copies the instance table to the device (synchronous); returns a cudaError_t
+    int (*batch_table_fill)(const BatchInstance* inst, uint32_t M, void* d_table, cudaStream_t s);
+    void (*b_vox_init)(const BatchArgs& b, int64_t* vox, cudaStream_t s);
+    void (*b_darts)(const BatchArgs& b, const CandArgs& c, cudaStream_t s);
+    void (*b_probe)(const BatchArgs& b, const CandArgs& c, int f32, int block, cudaStream_t s);
+    void (*b_collect)(const BatchArgs& b, const CandArgs& c, int f32, int block, cudaStream_t s);
+    void (*b_settle)(const BatchArgs& b, const CandArgs& c, int iteration, int f32, int block, cudaStream_t s);
+    void (*b_commit)(const BatchArgs& b, const CandArgs& c, cudaStream_t s);
+    void (*b_refine_mask)(const BatchArgs& b, const RefineArgs& a, int f32, int block, cudaStream_t s);
+    void (*b_refine_offsets)(const BatchArgs& b, const RefineArgs& a, uint64_t* new_off, cudaStream_t s);
+    void (*b_refine_write)(const BatchArgs& b, const RefineArgs& a, cudaStream_t s);
+    void (*b_results)(const BatchArgs& b, unsigned long long* counts, unsigned long long* sums, cudaStream_t s);
 };
 
 const DimOps* dim_ops(int D);

@@ -17,105 +17,13 @@
 #include "../../include/rsagpu.h"
 #include "rsa_device.cuh"
 #include "rsa_ops.h"
+#include "host_common.h"
 
 using namespace rsagpu;
+using namespace rsagpu::host;
 
-// ------------------------------------------------------------------------------------------------
-// errors
-// ------------------------------------------------------------------------------------------------
 namespace {
-thread_local std::string g_err;
-
-int fail(int code, const char* fmt, ...) {
-    char buf[1024];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof(buf), fmt, ap);
-    va_end(ap);
-    g_err = buf;
-    return code;
-}
-
-struct CudaError {
-    int code;
-};
-
-#define CK(call)                                                                                   \
-    do {                                                                                           \
-        cudaError_t e_ = (call);                                                                   \
-        if (e_ != cudaSuccess) {                                                                   \
-            fail(RSAGPU_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
-                 __LINE__);                                                                        \
-            throw CudaError{RSAGPU_ERR_CUDA};                                                      \
-        }                                                                                          \
-    } while (0)
-
-struct Fail {
-    int code;
-};
-
-[[noreturn]] void raise(int code, const char* fmt, ...) {
-    char buf[1024];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof(buf), fmt, ap);
-    va_end(ap);
-    g_err = buf;
-    throw Fail{code};
-}
-
-template <class F>
-int guarded(F&& f) {
-    try {
-        f();
-        return RSAGPU_OK;
-    } catch (const CudaError& e) {
-        return e.code;
-    } catch (const Fail& e) {
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        return fail(RSAGPU_ERR_CAPACITY, "host allocation failed");
-    }
-}
-
-template <class T>
-T* dalloc(uint64_t n) {
-    if (n == 0) n = 1;
-    void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        raise(RSAGPU_ERR_CUDA, "cudaMalloc of %llu bytes failed: %s", (unsigned long long)(n * sizeof(T)),
-              cudaGetErrorString(e));
-    }
-    return (T*)p;
-}
-
-template <class T>
-void dfree(T*& p) {
-    if (p) cudaFree(p);
-    p = nullptr;
-}
-
-// v_D(r) as volumeSphere (auxiliary/Geometry/Sphere.ixx:30-57): mult * puissance<D>(r)
-double pow_int(double x, int e) {
-    if (e == 0) return 1;
-    if (e == 1) return x;
-    int e1 = e / 2;
-    return pow_int(x, e1) * pow_int(x, e - e1);
-}
-double unit_ball_volume(int D) {
-    const double pi = 3.14159265358979323846;
-    double mult = 1;
-    if (D % 2 == 0) {
-        for (int k = 0; k <= D / 2 - 1; k++) mult *= (2 * pi) / (D - 2 * k);
-    } else {
-        mult = 1. / pi;
-        for (int k = 0; k <= (D - 1) / 2; k++) mult *= (2 * pi) / (D - 2 * k);
-    }
-    return mult;
-}
-double ball_volume(int D, double r) { return unit_ball_volume(D) * pow_int(r, D); }
+thread_local std::string g_err;  // text of rsagpu_last_error() for the calling thread
 
 // magical_default_miss_rate (operator_algorithm.ixx:344-351)
 double reference_miss_threshold(int D) { return D <= 3 ? 0.95 : 1 - 0.05 * pow_int(0.1, D - 3); }
@@ -241,8 +149,8 @@ struct rsagpu_algo {
     int form = RSAGPU_FORM_FP64, schedule = RSAGPU_SCHEDULE_HEURISTIC, cap_rule = RSAGPU_CAP_REFERENCE;
     // heuristic defaults tuned on config 2 (a sweep of factor x threshold): a quarter dart per voxel per pass,
     // refine when 99% of the darts miss
-    double factor = 0.25, miss_thr = 0.99;
-    uint64_t min_darts = 4096, max_darts = 1ull << 26;
+    double factor = kDefaultFactor, miss_thr = kDefaultMissThreshold;
+    uint64_t min_darts = kDefaultMinDarts, max_darts = kDefaultMaxDarts;
     std::vector<uint16_t> mlp;
     uint16_t* d_mlp = nullptr;      // the weights on the device
     float* d_feat = nullptr;        // features in, two outputs out
@@ -278,32 +186,26 @@ struct rsagpu_algo {
     }
 };
 
-namespace {
-
-void set_device(const rsagpu_domain* d) { CK(cudaSetDevice(d->device)); }
+namespace rsagpu {
+namespace host {
 
 // ------------------------------------------------------------------------------------------------
-// sphere grid: cells of edge c with c sqrt(D) < 2 r_min (at most one accepted centre per cell) and
+// sphere grid plan: cells of edge c with c sqrt(D) < 2 r_min (at most one accepted centre per cell) and
 // a stencil of every cell within 2 r_max (the largest centre distance any decision looks at).
 // ------------------------------------------------------------------------------------------------
-void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
-    const int D = dom->dim;
-    SphereGrid& G = dom->grid;
-    G.release();
-    G.rmin = rmin;
-    G.rmax = rmax;
-    GridArgs& a = G.a;
-    a = GridArgs{};
+GridPlan plan_grid(int D, const double* inf, const double* L, double rmin, double rmax) {
+    GridPlan P;
+    GridArgs& a = P.a;
     int64_t ncells = 1;
     double c[MAX_D];
     for (int d = 0; d < D; d++) {
-        int n = 1 + (int)(std::sqrt((double)D) * dom->L[d] / (2 * rmin));
-        while (dom->L[d] / n * std::sqrt((double)D) >= 2 * rmin * (1 - 1e-9)) n++;
+        int n = 1 + (int)(std::sqrt((double)D) * L[d] / (2 * rmin));
+        while (L[d] / n * std::sqrt((double)D) >= 2 * rmin * (1 - 1e-9)) n++;
         a.n[d] = n;
-        c[d] = dom->L[d] / n;
+        c[d] = L[d] / n;
         a.inv_c[d] = 1.0 / c[d];
-        a.inf[d] = dom->inf[d];
-        a.L[d] = dom->L[d];
+        a.inf[d] = inf[d];
+        a.L[d] = L[d];
         ncells *= n;
         if (ncells > (int64_t)1 << 40) raise(RSAGPU_ERR_CAPACITY, "cell grid too large");
     }
@@ -331,8 +233,9 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
             lb += t * t;
         }
         if (lb <= R * R * (1 + 1e-9)) {
-            std::vector<int8_t> v(D);
-            for (int d = 0; d < D; d++) v[d] = (int8_t)o[d];
+            std::vector<int8_t> v;
+            v.reserve(D);
+            for (int d = 0; d < D; d++) v.push_back((int8_t)o[d]);
             offs.push_back(v);
         }
         int d = 0;
@@ -350,12 +253,8 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
         }
         return nx < ny;
     });
-    G.stencil.clear();
-    for (auto& v : offs) G.stencil.insert(G.stencil.end(), v.begin(), v.end());
+    for (auto& v : offs) P.stencil.insert(P.stencil.end(), v.begin(), v.end());
     a.S = (int)offs.size();
-    G.d_stencil = dalloc<int8_t>(G.stencil.size());
-    CK(cudaMemcpy(G.d_stencil, G.stencil.data(), G.stencil.size(), cudaMemcpyHostToDevice));
-    a.stencil = G.d_stencil;
     // the same offsets as rows along dimension 0: for each (o_1..o_{D-1}) the contiguous range of o_0
     // (the bound is monotone in |o_0|), rows ordered by their nearest distance
     {
@@ -390,28 +289,13 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
         std::stable_sort(rows.begin(), rows.end(), [&](const std::vector<int8_t>& x, const std::vector<int8_t>& y) {
             return rest2(x) < rest2(y);
         });
-        G.rows.clear();
-        std::vector<float> r2;
         for (auto& r : rows) {
-            G.rows.insert(G.rows.end(), r.begin(), r.end());
-            r2.push_back((float)(rest2(r) * (1 - 1e-6)));  // rounded down: never drops a needed row
+            P.rows.insert(P.rows.end(), r.begin(), r.end());
+            P.rows_r2.push_back((float)(rest2(r) * (1 - 1e-6)));  // rounded down: never drops a needed row
         }
         a.R = (int)rows.size();
-        G.d_rows = dalloc<int8_t>(G.rows.size());
-        CK(cudaMemcpy(G.d_rows, G.rows.data(), G.rows.size(), cudaMemcpyHostToDevice));
-        a.rows = G.d_rows;
-        G.d_rows_r2 = dalloc<float>(r2.size());
-        CK(cudaMemcpy(G.d_rows_r2, r2.data(), r2.size() * sizeof(float), cudaMemcpyHostToDevice));
-        a.rows_r2 = G.d_rows_r2;
         a.rmax = rmax;
     }
-    // one padding word: the two-word window of occ_bits reads up to word nwords
-    const int64_t nwords = (ncells + 31) / 32 + 1;
-    a.occ = dalloc<uint32_t>(nwords);
-    a.pos = dalloc<double>((uint64_t)ncells * D);
-    a.rad = dalloc<double>(ncells);
-    a.off = dalloc<float>((uint64_t)ncells * D);
-    a.radf = dalloc<float>(ncells);
     {
         // Guard band of the FP32 screen: a bound, with a factor 4 to spare, on |FP32 model - FP64 value| of
         // every squared distance the kernels compare.  Per dimension the model o c_f + (off_s - off_q)
@@ -431,6 +315,48 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
         const double G = 4 * (D * E * (2 * Amax + E) + (D + 1) * u * D * Amax * Amax + 8 * u * (2 * rmax) * (2 * rmax));
         a.guard = (float)G;
     }
+    return P;
+}
+
+}  // namespace host
+}  // namespace rsagpu
+
+namespace {
+
+void set_device(const rsagpu_domain* d) { CK(cudaSetDevice(d->device)); }
+
+// ------------------------------------------------------------------------------------------------
+// sphere grid: cells of edge c with c sqrt(D) < 2 r_min (at most one accepted centre per cell) and
+// a stencil of every cell within 2 r_max (the largest centre distance any decision looks at).
+// ------------------------------------------------------------------------------------------------
+void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
+    const int D = dom->dim;
+    SphereGrid& G = dom->grid;
+    G.release();
+    G.rmin = rmin;
+    G.rmax = rmax;
+    GridPlan plan = plan_grid(D, dom->inf, dom->L, rmin, rmax);
+    GridArgs& a = G.a;
+    a = plan.a;
+    const int64_t ncells = a.ncells;
+    G.stencil = plan.stencil;
+    G.rows = plan.rows;
+    G.d_stencil = dalloc<int8_t>(G.stencil.size());
+    CK(cudaMemcpy(G.d_stencil, G.stencil.data(), G.stencil.size(), cudaMemcpyHostToDevice));
+    a.stencil = G.d_stencil;
+    G.d_rows = dalloc<int8_t>(G.rows.size());
+    CK(cudaMemcpy(G.d_rows, G.rows.data(), G.rows.size(), cudaMemcpyHostToDevice));
+    a.rows = G.d_rows;
+    G.d_rows_r2 = dalloc<float>(plan.rows_r2.size());
+    CK(cudaMemcpy(G.d_rows_r2, plan.rows_r2.data(), plan.rows_r2.size() * sizeof(float), cudaMemcpyHostToDevice));
+    a.rows_r2 = G.d_rows_r2;
+    // one padding word: the two-word window of occ_bits reads up to word nwords
+    const int64_t nwords = (ncells + 31) / 32 + 1;
+    a.occ = dalloc<uint32_t>(nwords);
+    a.pos = dalloc<double>((uint64_t)ncells * D);
+    a.rad = dalloc<double>(ncells);
+    a.off = dalloc<float>((uint64_t)ncells * D);
+    a.radf = dalloc<float>(ncells);
     a.phase = dalloc<int32_t>(ncells);
     G.head = dalloc<int32_t>(ncells);
     G.cocc = dalloc<uint32_t>(nwords);
@@ -775,7 +701,7 @@ bool end_round(rsagpu_algo* A, uint64_t n_shots, uint64_t n_new, bool* refined, 
         if (rg.n[rg.idx] == 0) rg.idx++;
     }
     const bool done = rg.idx >= (int)rg.n.size();
-    const double miss = (double)(n_shots - n_hits) / (0.000001 + (double)n_shots);
+    const double miss = miss_rate(n_shots, n_hits);
     *refined = false;
     bool do_refine = miss > thr;
     if (row) {
@@ -869,10 +795,7 @@ uint64_t darts_for(const rsagpu_algo* A) {
         const double m = std::min(1.0, A->nbshots / I);
         return std::max<uint64_t>(1, (uint64_t)std::llround(m * I));
     }
-    double c = A->factor * V;
-    c = std::max(c, (double)A->min_darts);
-    c = std::min(c, (double)A->max_darts);
-    return (uint64_t)c;
+    return heuristic_darts(A->factor, A->min_darts, A->max_darts, A->V);
 }
 
 void proceed(rsagpu_algo* A, uint64_t seed) {
@@ -895,11 +818,8 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         if (A->rg.idx >= (int)A->rg.n.size()) break;
         const uint64_t remaining = A->rg.n[A->rg.idx];
         uint64_t C = darts_for(A);
-        if (A->schedule != RSAGPU_SCHEDULE_REFERENCE) {
-            // no more than 16x the spheres still wanted of this class
-            const double cap = std::max(16.0 * (double)remaining, (double)A->min_darts);
-            if ((double)C > cap) C = (uint64_t)cap;
-        }
+        // no more than 16x the spheres still wanted of this class
+        if (A->schedule != RSAGPU_SCHEDULE_REFERENCE) C = cap_darts(C, remaining, A->min_darts);
         const bool may = C >= remaining;
         ensure_cand(A, C);
         reset_counters(A);
@@ -1457,12 +1377,6 @@ int rsagpu_algo_draw_darts(rsagpu_algo* algo, uint64_t seed, uint64_t round, uin
             CK(cudaMemcpyAsync(voxel_index, algo->cand.vidx, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, algo->stream));
         CK(cudaStreamSynchronize(algo->stream));
     });
-}
-
-int rsagpu_batch_run(const rsagpu_instance_desc* inst, int n, uint64_t* counts_out, double* fractions_out,
-                     double* seconds_out) {
-    return fail(RSAGPU_ERR_STATE, "batch form not built yet (%p %d %p %p %p)", (const void*)inst, n, (void*)counts_out,
-                (void*)fractions_out, (void*)seconds_out);
 }
 
 }  // extern "C"

@@ -236,3 +236,50 @@ class Algo:
 
 def kernel_launches() -> int:
     return int(lib().rsagpu_kernel_launches())
+
+
+def batch_run(instances, form: int = _lib.RSAGPU_FORM_FP32_GUARD, max_bytes: int = 0, autotune: bool = True):
+    """Runs independent one-radius instances to maximality in batched launches (rsagpu_batch_run).
+
+    instances: sequence of (dim, sup, radius, seed), the box being [0, sup].  Returns a dict with
+    per-instance ``counts``, ``checksums`` (see sphere_checksum) and ``seconds`` (time to maximality),
+    and the run's ``stats``.
+    """
+    n = len(instances)
+    arr = (_lib.InstanceDesc * max(n, 1))()
+    for i, (dim, sup, radius, seed) in enumerate(instances):
+        arr[i].dim = int(dim)
+        for d in range(min(int(dim), _lib.MAX_DIM, len(sup))):
+            arr[i].sup[d] = float(sup[d])
+        arr[i].radius = float(radius)
+        arr[i].seed = int(seed)
+    counts = np.zeros(max(n, 1), np.uint64)
+    sums = np.zeros(max(n, 1), np.uint64)
+    secs = np.zeros(max(n, 1))
+    st = _lib.BatchStats()
+    check(lib().rsagpu_batch_run(arr, n, int(form), int(max_bytes), 1 if autotune else 0, ptr(counts, _lib._u64),
+                                 ptr(sums, _lib._u64), ptr(secs, _lib._d), C.byref(st)))
+    stats = {k: getattr(st, k) for k, _ in _lib.BatchStats._fields_ if k != "block"}
+    stats["block"] = {d: list(st.block[d]) for d in range(2, _lib.MAX_DIM + 1) if any(st.block[d])}
+    return {"counts": counts[:n], "checksums": sums[:n], "seconds": secs[:n], "stats": stats}
+
+
+def _mix64(z: np.ndarray) -> np.ndarray:
+    z = z ^ (z >> np.uint64(30))
+    z = z * np.uint64(0xBF58476D1CE4E5B9)
+    z = z ^ (z >> np.uint64(27))
+    z = z * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def sphere_checksum(centers: np.ndarray) -> int:
+    """The order-free checksum rsagpu_batch_run reports for a set of centres (n x dim, FP64)."""
+    c = np.ascontiguousarray(centers, dtype=np.float64)
+    if c.size == 0:
+        return 0
+    bits = c.view(np.uint64).reshape(c.shape)
+    with np.errstate(over="ignore"):
+        h = np.full(c.shape[0], 0x9E3779B97F4A7C15, dtype=np.uint64)
+        for d in range(c.shape[1]):
+            h = _mix64(h ^ bits[:, d])
+        return int(h.sum(dtype=np.uint64))
