@@ -158,6 +158,73 @@ def run_e2e_step(dim, L, r, seed, form=1):
     return k, t1 - t0, pos.nbytes + rad.nbytes + phs.nbytes
 
 
+def run_learned_step(dim, L, r, seed, learned=True):
+    """One run of the FP32 form with the learned subdivision schedule (or the heuristic one)."""
+    from rsa_mpi_gb300 import _lib
+    from rsa_mpi_gb300 import schedule as S
+    _, wb = S.load()
+    out = S.run_case(dim, L, [(r, 1.0, 0)], seed,
+                     schedule=_lib.RSAGPU_SCHEDULE_LEARNED if learned else _lib.RSAGPU_SCHEDULE_HEURISTIC,
+                     weights_bf16=wb if learned else None)
+    return out["n"], out["stats"]
+
+
+def config4_instances(n=4096, seed=1):
+    """The batching workload: half 2D, half 3D, r = 0.01, box side log-uniform so that the expected counts
+    span 1e3 to 1e6 (2D side in [0.758, 23.97], 3D side in [0.2218, 2.218]); Philox key (seed, instance)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        dim = 2 if i < n // 2 else 3
+        lo, hi = (0.758, 23.97) if dim == 2 else (0.2218, 2.218)
+        s = float(np.exp(rng.uniform(math.log(lo), math.log(hi))))
+        out.append((dim, [s] * dim, 0.01, (seed << 32) | i))
+    return out
+
+
+def run_single_instances(inst, form):
+    """The instances one after another through the single-instance path: (spheres, device seconds)."""
+    from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator
+    n, ms = 0, 0.0
+    for dim, sup, r, seed in inst:
+        rg = RadiusGenerator(dim, [(r, 1.0, 0)], volume=float(math.prod(sup)))
+        dom = Domain([0.0] * dim, sup, r)
+        a = Algo(dom, rg, 6000)
+        a.set_form(form)
+        a.proceed(seed)
+        ms += a.stats()["ms_total"]
+        n += dom.count()
+        a.close()
+        dom.close()
+    return n, ms * 1e-3
+
+
+def batched_form():
+    """Config 4 through rsagpu_batch_run, and a 64-instance sample of it run both ways and in both forms."""
+    from rsa_mpi_gb300.sampler import batch_run
+    inst = config4_instances()
+    res = batch_run(inst, form=1)
+    total = int(res["counts"].sum())
+    st = res["stats"]
+    sample = inst[::64]
+    cmp = {}
+    for form, name in ((0, "fp64"), (1, "fp32")):
+        batch_run(sample, form=form)  # warm
+        r2 = batch_run(sample, form=form)
+        n1, s1 = run_single_instances(sample, form)
+        cmp[name] = {"batched_s": r2["stats"]["seconds"], "single_s": s1, "spheres": n1,
+                     "same_counts": int(r2["counts"].sum()) == n1}
+    base = cmp["fp64"]["spheres"] / cmp["fp64"]["single_s"]
+    return {"workload": "4096 instances, half 2D / half 3D, r=0.01, log-uniform box sides, FP32 form",
+            "spheres_per_s": total / st["seconds"], "seconds": st["seconds"], "spheres": total,
+            "waves": st["waves"], "rounds": st["rounds"], "launches": st["launches"], "block_shapes": st["block"],
+            "sample_every_64th": cmp,
+            "speedup_vs_fp64": (cmp["fp32"]["spheres"] / cmp["fp32"]["batched_s"]) / base,
+            "speedup_vs_fp64_note": "sample of 64 instances: batched FP32 vs the single-instance plain FP64 form, "
+                                    "one instance after another"}
+
+
 def cpu_sample(dim, L, r, seed):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -274,6 +341,18 @@ def main():
         base = forms[FORM_NAMES[0]]["spheres_per_s"]
         for v in forms.values():
             v["speedup_vs_fp64"] = v["spheres_per_s"] / base
+        # learned subdivision schedule (FP32 form), on this workload and on the 4D r = 0.02 hypercube
+        nl, stl = run_learned_step(dim, L, r, seed, True)
+        learned = {"spheres_per_s": nl / (stl["ms_total"] * 1e-3), "ms": stl["ms_total"], "rounds": stl["rounds"],
+                   "refinements": stl["refinements"], "spheres": nl}
+        learned["speedup_vs_fp64"] = learned["spheres_per_s"] / base
+        h4 = min((run_learned_step(4, [1.0] * 4, 0.02, 5, False) for _ in range(3)), key=lambda t: t[1]["ms_total"])
+        l4 = min((run_learned_step(4, [1.0] * 4, 0.02, 5, True) for _ in range(3)), key=lambda t: t[1]["ms_total"])
+        learned["4D r=0.02 (held out)"] = {"heuristic_ms": h4[1]["ms_total"], "learned_ms": l4[1]["ms_total"],
+                                           "heuristic_rounds": h4[1]["rounds"], "learned_rounds": l4[1]["rounds"],
+                                           "heuristic_spheres": h4[0], "learned_spheres": l4[0]}
+        forms["learned schedule (FP32 form)"] = learned
+        forms["batched (config 4)"] = batched_form()
 
     # e2e through the C ABI with host buffers
     e2e_n, e2e_s, d2h = 0, 0.0, 0

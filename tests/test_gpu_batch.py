@@ -51,7 +51,7 @@ def test_batch_instances_equal_their_single_runs(form):
 def test_batch_results_do_not_depend_on_waves_or_block_shapes():
     inst = instances(6, 6, seed=9)
     a = batch_run(inst, autotune=True)
-    b = batch_run(inst, max_bytes=1 << 20, autotune=False)  # a budget below one instance: a wave each
+    b = batch_run(inst, max_bytes=1, autotune=False)  # a budget below any instance: one wave each
     assert a["stats"]["waves"] == 2 and b["stats"]["waves"] == len(inst)
     np.testing.assert_array_equal(a["counts"], b["counts"])
     np.testing.assert_array_equal(a["checksums"], b["checksums"])
