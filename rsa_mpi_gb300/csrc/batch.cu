@@ -370,6 +370,7 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
             for (int d = 0; d < D; d++) {
                 rnd[s].len[d] = x.len[d];
                 rnd[s].nlen[d] = 0.5 * x.len[d];
+                voxel_cell_ratio(x.len[d], x.plan.a.c[d], &rnd[s].rho_int[d], &rnd[s].rho_frac[d]);
             }
             rnd[s].refine = 0;
         }
@@ -488,7 +489,14 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
             const int other = 1 - cur;
             ensure_vox(W, D, other, total);
             ra.vout = W.vox[other];
+            ra.vout_cap = total;
             ops->b_refine_write(b, ra, st);
+            {
+                uint32_t err = 0;
+                CK(cudaMemcpyAsync(&err, W.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                if (err & ERR_WRITE_BOUNDS) raise(RSAGPU_ERR_INVARIANT, "refinement offsets beyond the output list");
+            }
             cur = other;
             Vtot = total;
             std::swap(W.vox_off, W.new_off);

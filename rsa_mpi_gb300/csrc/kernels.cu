@@ -535,6 +535,7 @@ struct RefineParams {
     uint64_t V;
     const int64_t* vin;
     int64_t* vout;
+    uint64_t vout_cap;
     double len[D];
     double nlen[D];
     double inf[D];
@@ -549,6 +550,8 @@ struct RefineParams {
     float lenf[D];
     float nlenf[D];
     float rminf;
+    uint64_t rho_frac[D];  // len / c: 64-bit fraction and integer part (FP32 form's voxel-to-cell map)
+    uint32_t rho_int[D];
 };
 
 // child index with bit d = offset along dimension d, for the child at position t of the corner table
@@ -754,21 +757,34 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
                                                    const int64_t* cc, uint32_t* mask, uint32_t& visits, uint32_t& rt) {
     bool survived = false;
     {
-        double orig[D], centre[D];
         float relo[D], relc[D];
         int32_t k[D];
 #pragma unroll
         for (int d = 0; d < D; d++) {
-            orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cc[d], p.len[d]));
-            centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cc[d], 0.5), p.len[d]));
+            // The voxel centre in cell edges, y = (cc + 1/2) len / c, as the 64-bit fixed-point product
+            // (2 cc + 1) * rho / 2 (rho = len / c, integer part and 64-bit fraction): its integer part is the
+            // cell, its fraction the centre's offset from the cell's corner.  Integer instructions only; the
+            // FP64 pipe of this GPU runs at 1/64 of the FP32 rate.  The error (below 2^-29 cell edges) is
+            // inside the guard band, and only the screen uses these values.
+            const uint64_t m = 2 * (uint64_t)cc[d] + 1;
+            const uint64_t hi = __umul64hi(m, p.rho_frac[d]);
+            const uint64_t lo = m * p.rho_frac[d];
+            const uint64_t two_y = m * (uint64_t)p.rho_int[d] + hi;  // floor(2 y)
+            int64_t kd = (int64_t)(two_y >> 1);
+            const uint32_t fb = ((uint32_t)(two_y & 1u) << 31) | (uint32_t)(lo >> 33);  // frac(y) in 2^-32
+            if (kd >= g.n[d]) kd -= g.n[d];  // the top face rounds onto the periodic image of cell 0
+            k[d] = (int32_t)(kd < g.n[d] ? kd : g.n[d] - 1);
+            relc[d] = __fmul_rn(__fmul_rn(__uint2float_rn(fb), 0x1p-32f), g.cf[d]);
+            relo[d] = __fsub_rn(relc[d], __fmul_rn(0.5f, p.lenf[d]));
         }
-        cell_of<D>(g, geo, centre, k);
+        // the exact FP64 origin and centre (list_of_voxels.ixx:154-160), for the guard band only
+        auto exact_corners = [&](double* orig, double* centre) {
 #pragma unroll
-        for (int d = 0; d < D; d++) {
-            const double base = __dadd_rn(geo.inf[d], __dmul_rn((double)k[d], g.c[d]));
-            relo[d] = __double2float_rn(__dsub_rn(orig[d], base));
-            relc[d] = __double2float_rn(__dsub_rn(centre[d], base));
-        }
+            for (int d = 0; d < D; d++) {
+                orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cc[d], p.len[d]));
+                centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cc[d], 0.5), p.len[d]));
+            }
+        };
         float pre0[K_PRE][D], pre1[K_PRE][D], preR2[K_PRE];
         int64_t preidx[K_PRE];
         uint32_t preq[K_PRE];  // 2 bits per dimension: image shift + 1
@@ -776,10 +792,11 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
         bool overflow = false;
         // exact FP64 differences of one (voxel, sphere) pair, for the guard band
         auto exact_deltas = [&](int64_t idx, const int8_t* q, double* dl0, double* dl1) {
-            double pp[D], img[D];
+            double pp[D], img[D], orig[D], centre[D];
 #pragma unroll
             for (int d = 0; d < D; d++) pp[d] = g.pos[idx * D + d];
             image_of<D>(geo, pp, q, img);
+            exact_corners(orig, centre);
 #pragma unroll
             for (int d = 0; d < D; d++) {
                 dl0[d] = __dsub_rn(img[d], orig[d]);
@@ -897,6 +914,8 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
                 // the list was full: every prefilter sphere again, in FP64, straight from the grid
 #pragma unroll
                 for (int w = 0; w < MASK_WORDS; w++) cov[w] = 0;
+                double orig[D], centre[D];
+                exact_corners(orig, centre);
                 visit_placed<D>(g, geo, k, R2q, [&](int64_t idx, const double* img, double rs) {
                     const double R = __dadd_rn(rs, p.rmin);
                     const uint64_t R2b = dbits(__dmul_rn(R, R));
@@ -979,6 +998,10 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
     }
     if (v >= p.V || cnt == 0) return;
     uint64_t o = p.warp_offsets[v >> 5] + (incl - cnt);
+    if (o + cnt > p.vout_cap) {
+        atomicOr(p.err, (uint32_t)ERR_WRITE_BOUNDS);
+        return;
+    }
     int64_t cc[D];
 #pragma unroll
     for (int d = 0; d < D; d++) cc[d] = p.vin[v * D + d];
@@ -1150,6 +1173,7 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
     p.V = a.V;
     p.vin = a.vin;
     p.vout = a.vout;
+    p.vout_cap = a.vout_cap;
     for (int d = 0; d < D; d++) {
         p.len[d] = a.len[d];
         p.nlen[d] = a.nlen[d];
@@ -1166,6 +1190,8 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
     for (int d = 0; d < D; d++) {
         p.lenf[d] = (float)a.len[d];
         p.nlenf[d] = (float)a.nlen[d];
+        p.rho_frac[d] = a.rho_frac[d];
+        p.rho_int[d] = a.rho_int[d];
     }
     p.rminf = (float)a.rmin;
     return p;

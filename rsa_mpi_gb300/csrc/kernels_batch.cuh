@@ -201,6 +201,8 @@ __global__ void __launch_bounds__(512, 2) k_b_refine_mask(BatchArgs b, RefineArg
                 p.inf[d] = geo.inf[d];
                 p.lenf[d] = (float)R.len[d];
                 p.nlenf[d] = (float)R.nlen[d];
+                p.rho_frac[d] = R.rho_frac[d];
+                p.rho_int[d] = R.rho_int[d];
             }
             p.rmin = g.rmono;
             p.rminf = (float)g.rmono;
@@ -276,6 +278,10 @@ __global__ void __launch_bounds__(256) k_b_refine_write(BatchArgs b, RefineArgs 
     }
     if (v >= b.V || cnt == 0) return;
     uint64_t o = a.warp_offsets[v >> 5] + (incl - cnt);
+    if (o + cnt > a.vout_cap) {
+        atomicOr(a.err, (uint32_t)ERR_WRITE_BOUNDS);
+        return;
+    }
     int64_t cc[D];
 #pragma unroll
     for (int d = 0; d < D; d++) cc[d] = a.vin[v * D + d];

@@ -10,29 +10,100 @@ namespace {
 std::atomic<uint64_t> g_launches{0};
 
 constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 8;                            // counts per thread
+constexpr uint64_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // counts per block
 
-// Exclusive scan of n uint32 counts into uint64 offsets with one block; total in offsets[n].
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_blocks(const uint32_t* counts, uint64_t* offsets, uint64_t n) {
-    __shared__ uint64_t sh[SCAN_THREADS];
-    const uint64_t chunk = (n + SCAN_THREADS - 1) / SCAN_THREADS;
-    const uint64_t b = threadIdx.x * chunk;
-    const uint64_t e = b + chunk < n ? b + chunk : n;
-    uint64_t sum = 0;
-    for (uint64_t i = b; i < e; i++) sum += counts[i];
-    sh[threadIdx.x] = sum;
+// Exclusive scan of n uint32 counts into uint64 offsets (total in offsets[n]) in three passes over tiles of
+// SCAN_TILE counts: the tile sums are parked in the first offset slot of each tile (which the last pass
+// overwrites), scanned by one block, then every tile is scanned from its base.
+__device__ __forceinline__ uint32_t load_items(const uint32_t* counts, uint64_t n, uint64_t i0, uint32_t* v) {
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        v[k] = i0 + k < n ? counts[i0 + k] : 0u;
+        sum += v[k];
+    }
+    return sum;
+}
+
+// exclusive scan over the block's SCAN_THREADS threads; *total (if given) = the block's sum, for every thread
+__device__ __forceinline__ uint64_t block_scan64(uint64_t x, uint64_t* total) {
+    __shared__ uint64_t warp_sums[SCAN_THREADS / 32];
+    __shared__ uint64_t block_total;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
     __syncthreads();
-    for (int o = 1; o < SCAN_THREADS; o <<= 1) {
-        uint64_t y = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+    if (warp == 0) {
+        uint64_t w = warp_sums[lane];
+        uint64_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        warp_sums[lane] = wi - w;
+        if (lane == 31) block_total = wi;
+    }
+    __syncthreads();
+    const uint64_t r = warp_sums[warp] + incl - x;
+    if (total) *total = block_total;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_sums(const uint32_t* counts, uint64_t* offsets, uint64_t n) {
+    const uint64_t i0 = blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint64_t s = load_items(counts, n, i0, v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ uint64_t ws[SCAN_THREADS / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint64_t t = ws[threadIdx.x];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) offsets[blockIdx.x * SCAN_TILE] = t;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_bases(uint64_t* offsets, uint64_t n, uint64_t tiles) {
+    __shared__ uint64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint64_t b = 0; b < tiles; b += SCAN_THREADS) {
+        const uint64_t t = b + threadIdx.x;
+        const uint64_t x = t < tiles ? offsets[t * SCAN_TILE] : 0;
+        uint64_t chunk;
+        const uint64_t ex = block_scan64(x, &chunk);
+        if (t < tiles) offsets[t * SCAN_TILE] = carry + ex;
         __syncthreads();
-        sh[threadIdx.x] += y;
+        if (threadIdx.x == 0) carry += chunk;
         __syncthreads();
     }
-    uint64_t run = sh[threadIdx.x] - sum;
-    for (uint64_t i = b; i < e; i++) {
-        offsets[i] = run;
-        run += counts[i];
+    if (threadIdx.x == 0) offsets[n] = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(const uint32_t* counts, uint64_t* offsets, uint64_t n) {
+    __shared__ uint64_t base;
+    if (threadIdx.x == 0) base = offsets[blockIdx.x * SCAN_TILE];
+    __syncthreads();
+    const uint64_t i0 = blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    const uint32_t s = load_items(counts, n, i0, v);
+    uint64_t run = base + block_scan64(s, nullptr);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        if (i0 + k < n) offsets[i0 + k] = run;
+        run += v[k];
     }
-    if (threadIdx.x == SCAN_THREADS - 1) offsets[n] = sh[SCAN_THREADS - 1];
 }
 
 __global__ void __launch_bounds__(OCC_BLOCK) k_occ_block_counts(const uint32_t* occ, int64_t nwords, uint32_t* counts) {
@@ -49,8 +120,11 @@ uint64_t kernel_launch_count() { return g_launches.load(); }
 
 void launch_scan_blocks(const uint32_t* counts, uint64_t* offsets, uint64_t n, uint64_t* total, cudaStream_t s) {
     (void)total;
-    k_scan_blocks<<<1, SCAN_THREADS, 0, s>>>(counts, offsets, n);
-    count_launch();
+    const uint64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (tiles) k_scan_tile_sums<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(counts, offsets, n);
+    k_scan_tile_bases<<<1, SCAN_THREADS, 0, s>>>(offsets, n, tiles);
+    if (tiles) k_scan_tiles<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(counts, offsets, n);
+    count_launch(tiles ? 3 : 1);
 }
 
 void launch_occ_block_counts(const uint32_t* occ, int64_t nwords, uint32_t* counts, cudaStream_t s) {

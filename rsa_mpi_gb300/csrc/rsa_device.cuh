@@ -26,6 +26,7 @@ enum : uint32_t {
     ERR_DOUBLE_OCCUPANCY = 1u,   // two accepted centres in one cell
     ERR_BLOCKER_OVERFLOW = 2u,   // (informational) a candidate had more than NB lower colliders
     ERR_PREFILTER_OVERFLOW = 4u, // (informational) a parent voxel had more than K prefilter spheres
+    ERR_WRITE_BOUNDS = 8u,       // a refinement output offset beyond the output buffer (write skipped)
 };
 
 constexpr int NB = 24;     // stored lower-priority colliders per candidate (more: rescan)

@@ -3,6 +3,7 @@
 // (rsagpu.cu) picks the table for the instance's dimension.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -72,6 +73,7 @@ struct RefineArgs {
     uint64_t V;
     const int64_t* vin;
     int64_t* vout;
+    uint64_t vout_cap;   // voxels vout holds
     double len[MAX_D];   // parent length
     double nlen[MAX_D];  // child length = 0.5 * parent
     double rmin;
@@ -82,7 +84,18 @@ struct RefineArgs {
     uint32_t* survivors;  // parents not covered (remove_covered keeps them)
     unsigned long long* visits;  // occupied stencil cells visited by the mask pass
     unsigned long long* retests; // (voxel, sphere) pairs redone in FP64 (guard-band form)
+    uint64_t rho_frac[MAX_D];    // len / c in 64-bit fixed point (voxel_cell_ratio)
+    uint32_t rho_int[MAX_D];
 };
+
+// len / c (voxel length in cell edges) as an integer part and a 64-bit fraction, for the FP32 form's
+// fixed-point map from voxel coordinates to cells
+inline void voxel_cell_ratio(double len, double c, uint32_t* rho_int, uint64_t* rho_frac) {
+    const double rho = len / c;
+    const double ip = std::floor(rho);
+    *rho_int = (uint32_t)ip;
+    *rho_frac = (uint64_t)std::ldexp(rho - ip, 64);  // rho - ip <= 1 - 2^-53: below 2^64
+}
 
 // ------------------------------------------------------------------------------------------------
 // batched instances: many independent one-radius instances of one dimension share every launch.
@@ -102,6 +115,8 @@ struct BatchRound {      // per instance, per round
     uint64_t V;          // voxels in its segment
     double len[MAX_D];   // voxel length at its level
     double nlen[MAX_D];  // child length = 0.5 * len
+    uint64_t rho_frac[MAX_D];  // len / c (voxel_cell_ratio)
+    uint32_t rho_int[MAX_D];
     int32_t refine;      // subdivide its voxels after this round's pass
 };
 

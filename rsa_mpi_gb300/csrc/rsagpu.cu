@@ -301,7 +301,9 @@ GridPlan plan_grid(int D, const double* inf, const double* L, double rmin, doubl
         // every squared distance the kernels compare.  Per dimension the model o c_f + (off_s - off_q)
         // errs by at most E (float rounding of c, of the offsets, of the product and of the two sums, and of
         // a voxel length); every difference is below A; the squares and the D-term sum add (D+1) roundings of
-        // a quantity below D A^2; the threshold (r_s + r_q)^2 in float adds 8 ulps of (2 r_max)^2.
+        // a quantity below D A^2; the threshold (r_s + r_q)^2 in float adds 8 ulps of (2 r_max)^2.  The voxel
+        // offsets of the mask pass come from a fixed-point cell map (error below 2^-29 c) and two more float
+        // roundings (the centre's offset, then the origin's = centre's - len / 2): u (4 c + 2 len) more.
         const double u = std::ldexp(1.0, -24);
         double cmax = 0;
         int wmax = 0;
@@ -310,7 +312,7 @@ GridPlan plan_grid(int D, const double* inf, const double* L, double rmin, doubl
             wmax = std::max(wmax, w[d]);
         }
         const double lmax = (rmax + rmin) / std::sqrt((double)D);  // level-0 voxel length bound
-        const double E = u * cmax * (4 * wmax + 8) + u * lmax;
+        const double E = u * cmax * (4 * wmax + 8) + u * lmax + u * (4 * cmax + 2 * lmax);
         const double Amax = (wmax + 1) * cmax + lmax;
         const double G = 4 * (D * E * (2 * Amax + E) + (D + 1) * u * D * Amax * Amax + 8 * u * (2 * rmax) * (2 * rmax));
         a.guard = (float)G;
@@ -478,6 +480,7 @@ void refine(rsagpu_algo* A) {
     for (int d = 0; d < D; d++) {
         r.len[d] = A->len[d];
         r.nlen[d] = 0.5 * A->len[d];
+        voxel_cell_ratio(A->len[d], A->dom->grid.a.c[d], &r.rho_int[d], &r.rho_frac[d]);
     }
     r.rmin = A->rg.rmin();
     r.masks = A->masks;
@@ -527,7 +530,14 @@ void refine(rsagpu_algo* A) {
     const int other = 1 - A->cur;
     ensure_vox(A, other, total);
     r.vout = A->vox[other];
+    r.vout_cap = total;
     A->ops->refine_write(r, A->stream);
+    {
+        uint32_t err = 0;
+        CK(cudaMemcpyAsync(&err, r.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
+        CK(cudaStreamSynchronize(A->stream));
+        if (err & ERR_WRITE_BOUNDS) raise(RSAGPU_ERR_INVARIANT, "refinement offsets beyond the output list");
+    }
     A->cur = other;
     A->V = total;
     A->level++;
