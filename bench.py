@@ -225,6 +225,34 @@ def batched_form():
                                     "one instance after another"}
 
 
+def precision_form():
+    """Config 3 (3D unit cube, radii 0.004 / 0.002 / 0.001 at volume fractions 0.20 / 0.10 / 0.05, seed 1) in the
+    plain FP64 form and the FP32 guard-band form: the same spheres (count and centre checksum), the FP64 retests."""
+    import numpy as np
+    from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator, sphere_checksum
+    classes = [(0.004, 0.20, 0), (0.002, 0.10, 0), (0.001, 0.05, 0)]
+    out = {}
+    for form in (0, 1):
+        rg = RadiusGenerator(3, classes, volume=1.0)
+        dom = Domain([0.0] * 3, [1.0] * 3, 0.004)
+        a = Algo(dom, rg, 6000)
+        a.set_form(form)
+        a.proceed(1)
+        st = a.stats()
+        pos, rad, _ = dom.arrays()
+        out[form] = {"spheres": int(len(rad)), "ms": st["ms_total"], "retests": st["retests"],
+                     "per_class": [int(np.count_nonzero(rad == r)) for r, _, _ in classes],
+                     "checksum": sphere_checksum(pos), "maximal": st["maximal"]}
+        a.close()
+        dom.close()
+    return {"workload": "3D unit cube, radii 0.004/0.002/0.001, fractions 0.20/0.10/0.05, seed 1",
+            "fp64": out[0], "fp32_guard": out[1],
+            "same_spheres": out[0]["checksum"] == out[1]["checksum"] and out[0]["spheres"] == out[1]["spheres"],
+            "spheres_per_s_fp64": out[0]["spheres"] / (out[0]["ms"] * 1e-3),
+            "spheres_per_s_fp32_guard": out[1]["spheres"] / (out[1]["ms"] * 1e-3),
+            "speedup_vs_fp64": out[0]["ms"] / out[1]["ms"]}
+
+
 def cpu_sample(dim, L, r, seed):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -353,6 +381,7 @@ def main():
                                            "heuristic_spheres": h4[0], "learned_spheres": l4[0]}
         forms["learned schedule (FP32 form)"] = learned
         forms["batched (config 4)"] = batched_form()
+        forms["FP32 guard band, polydisperse (config 3)"] = precision_form()
 
     # e2e through the C ABI with host buffers
     e2e_n, e2e_s, d2h = 0, 0.0, 0

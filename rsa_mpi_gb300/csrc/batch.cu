@@ -74,6 +74,9 @@ struct Wave {
     uint64_t vox_cap[2] = {0, 0};
     uint32_t* masks = nullptr;
     uint64_t masks_cap = 0;
+    uint32_t* bin_hist = nullptr;  // binned dart order
+    uint64_t* bin_off = nullptr;
+    uint64_t bins_cap = 0;
     uint32_t* warp_counts = nullptr;
     uint64_t* warp_offsets = nullptr;
     uint64_t warps_cap = 0;
@@ -82,6 +85,7 @@ struct Wave {
     // candidates
     CandArgs c{};
     uint32_t* cinst = nullptr;
+    uint32_t* perm = nullptr;  // binned dart order
     uint64_t cand_cap = 0;
     ~Wave() {
         dfree(occ);
@@ -103,6 +107,8 @@ struct Wave {
         dfree(vox[0]);
         dfree(vox[1]);
         dfree(masks);
+        dfree(bin_hist);
+        dfree(bin_off);
         dfree(warp_counts);
         dfree(warp_offsets);
         dfree(err);
@@ -124,6 +130,7 @@ struct Wave {
         dfree(c.blk);
         dfree(c.nblk);
         dfree(cinst);
+        dfree(perm);
         cand_cap = 0;
     }
 };
@@ -153,6 +160,7 @@ void ensure_cand(Wave& W, int D, bool f32, uint64_t n) {
     W.c.blk = dalloc<int32_t>(cap * NB);
     W.c.nblk = dalloc<uint8_t>(cap);
     W.cinst = dalloc<uint32_t>(cap);
+    W.perm = dalloc<uint32_t>(cap);
     W.cand_cap = cap;
 }
 
@@ -370,8 +378,12 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
             for (int d = 0; d < D; d++) {
                 rnd[s].len[d] = x.len[d];
                 rnd[s].nlen[d] = 0.5 * x.len[d];
-                voxel_cell_ratio(x.len[d], x.plan.a.c[d], &rnd[s].rho_int[d], &rnd[s].rho_frac[d]);
+                if (!voxel_cell_ratio(x.len[d], x.level, x.plan.a.c[d], x.plan.a.n[d], &rnd[s].rho_int[d],
+                                      &rnd[s].rho_frac[d]))
+                    raise(RSAGPU_ERR_CAPACITY, "instance %d: level %d too deep for the fixed-point cell map", x.user,
+                          x.level);
             }
+            rnd[s].level = x.level;
             rnd[s].refine = 0;
         }
         const uint64_t ndarts = dart_off[M];
@@ -391,7 +403,28 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
         b.ndarts = ndarts;
         b.vox = W.vox[cur];
         b.V = Vtot;
-        ops->b_darts(b, c, st);
+        c.lazy = f32 ? 1 : 0;  // FP32 form: lazy candidates (positions formed in the probe when needed)
+        {
+            // binned order over the wave's voxel list: the darts are written grouped by voxel region
+            b.bin_shift = dart_bin_shift(Vtot, ndarts);
+            const uint64_t nbins = ((Vtot - 1) >> b.bin_shift) + 1;
+            if (nbins > W.bins_cap) {
+                dfree(W.bin_hist);
+                dfree(W.bin_off);
+                W.bins_cap = std::max<uint64_t>(nbins, W.bins_cap + W.bins_cap / 2);
+                W.bin_hist = dalloc<uint32_t>(W.bins_cap);
+                W.bin_off = dalloc<uint64_t>(W.bins_cap + 1);
+            }
+            CK(cudaMemsetAsync(W.bin_hist, 0, nbins * sizeof(uint32_t), st));
+            b.bin_hist = W.bin_hist;
+            b.bin_off = nullptr;
+            b.perm = W.perm;
+            ops->b_dart_bins(b, c, st);  // histogram
+            launch_scan_blocks(W.bin_hist, W.bin_off, nbins, nullptr, st);
+            b.bin_off = W.bin_off;
+            ops->b_dart_bins(b, c, st);  // permutation
+        }
+        ops->b_darts(b, c, f, st);
         const int bp = tuner.pick(0), bc = tuner.pick(1), bs = tuner.pick(2);
         CK(cudaEventRecord(ev.e[0], st));
         ops->b_probe(b, c, f, bp, st);
@@ -417,6 +450,7 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
         CK(cudaMemcpyAsync(h_acc, W.acc, M * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         if (h_cnt[2] & ERR_DOUBLE_OCCUPANCY) raise(RSAGPU_ERR_INVARIANT, "two accepted centres in one grid cell");
+        if (h_cnt[2] & ERR_DART_SLOT) raise(RSAGPU_ERR_INVARIANT, "binned dart order: a bin overflowed");
         {
             const double alive = (double)h_cnt[0];
             tuner.record(0, ev.ms(0, 1), (double)ndarts);

@@ -134,6 +134,14 @@ inline double miss_rate(uint64_t shots, uint64_t hits) {
     return (double)(shots - hits) / (0.000001 + (double)shots);
 }
 
+// Binned dart order: bins of 2^shift consecutive voxels, about 64 darts per bin (the voxel list is in spatial
+// order, so a bin is a small region of the box and the probe's neighbouring threads share stencil cells).
+inline int dart_bin_shift(uint64_t V, uint64_t darts) {
+    int sh = 0;
+    while (sh < 48 && (double)darts * std::ldexp(1.0, sh) < 64.0 * (double)V) sh++;
+    return sh;
+}
+
 // Geometry of a sphere grid: the cell counts, the stencil, its rows and the FP32 guard band.  Both drivers
 // build every grid through this one function, so a batched instance gets exactly the grid of its
 // single-instance run.

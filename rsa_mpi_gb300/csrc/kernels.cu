@@ -117,13 +117,46 @@ struct DartParams {
     int32_t* cphase;
     uint8_t* state;
     uint64_t* vidx_out;
+    // FP32 form: the candidate's cell and FP32 offsets from a fixed-point map, the exact position deferred
+    int32_t* kc;
+    float* off;
+    int64_t* cell;
+    uint64_t rho_frac[D];  // level-0 voxel length / cell edge (voxel_cell_ratio)
+    uint32_t rho_int[D];
+    int32_t level;         // voxel level (fixed-point shift)
+    int32_t ncell[D];      // cells per dimension
+    float cf[D];           // cell edge rounded to float
+    // binned order (optional): slot t holds dart perm[t]; perm lists the darts bin by bin, bin b =
+    // (vbase + voxel) >> bin_shift, so that neighbouring threads of the probe hold neighbouring darts
+    uint32_t* bin_hist;
+    const uint64_t* bin_off;
+    int32_t bin_shift;
+    uint64_t vbase;        // first voxel of this list in the binned index space
+    uint32_t* perm;
+    uint32_t* err;         // error bits (ERR_DART_SLOT)
 };
 
-// Dart i of the round (counter (i, round, call) under the run's key), written to candidate slot o.
-__device__ __forceinline__ void dart_body(const DartParams& p, uint32_t i, uint64_t o) {
-    constexpr int WORDS = 2 + 2 * D + 1;
-    constexpr int CALLS = (WORDS + 3) / 4;
-    uint32_t w[CALLS * 4];
+// voxel drawn by dart i (the first Philox call's words 0 and 1)
+__device__ __forceinline__ uint64_t dart_voxel(const DartParams& p, uint32_t i) {
+    const uint4 r = philox4x32_10(make_uint4(i, p.round_lo, p.round_hi, 0u), make_uint2(p.seed_lo, p.seed_hi));
+    return __umul64hi(((uint64_t)r.x << 32) | r.y, p.V);
+}
+
+// places dart i (index t in perm's index space) in its bin: perm[bin_off[b] + rank] = t.  A full bin (which
+// the histogram pass rules out) raises ERR_DART_SLOT and places nothing.
+__device__ __forceinline__ void place_dart(const DartParams& p, uint32_t i, uint32_t t) {
+    const uint64_t b = (p.vbase + dart_voxel(p, i)) >> p.bin_shift;
+    const uint32_t left = atomicSub(p.bin_hist + b, 1u);
+    if (left == 0u) {
+        atomicOr(p.err, (uint32_t)ERR_DART_SLOT);
+        return;
+    }
+    p.perm[p.bin_off[b] + (left - 1u)] = t;
+}
+
+// Philox words of dart i: [0, 1] voxel draw, [2 + 2d, 3 + 2d] coordinate d, [2 + 2D] priority
+template <int CALLS>
+__device__ __forceinline__ void dart_words(const DartParams& p, uint32_t i, uint32_t* w) {
     const uint2 k = make_uint2(p.seed_lo, p.seed_hi);
 #pragma unroll
     for (int c = 0; c < CALLS; c++) {
@@ -133,6 +166,46 @@ __device__ __forceinline__ void dart_body(const DartParams& p, uint32_t i, uint6
         w[4 * c + 2] = r.z;
         w[4 * c + 3] = r.w;
     }
+}
+
+// FP32 form of a dart: the same voxel, coordinates and priority as dart_body, but the FP64 position is not
+// formed (that is 7 FP64 instructions per coordinate, each costing 64 FP32 ones on this GPU).  Instead:
+//  * cell and FP32 offset from the exact dart y = (cc + u) len / c in fixed point (fixed_cell: integer part =
+//    cell, fraction = offset; error below 2^-31 cell edges, far inside the guard band);
+//  * the inputs of the exact position kept for later: the voxel index in cell[o] and the 53 random bits of
+//    each coordinate in pos[o] (lazy_position forms the FP64 position for the candidates that need it).
+__device__ __forceinline__ void dart32_body(const DartParams& p, uint32_t i, uint64_t o) {
+    constexpr int WORDS = 2 + 2 * D + 1;
+    constexpr int CALLS = (WORDS + 3) / 4;
+    uint32_t w[CALLS * 4];
+    dart_words<CALLS>(p, i, w);
+    const uint64_t r64 = ((uint64_t)w[0] << 32) | w[1];
+    const uint64_t v = __umul64hi(r64, p.V);
+    p.cell[o] = (int64_t)v;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const uint64_t bits = (((uint64_t)w[2 + 2 * d] << 32) | w[3 + 2 * d]) >> 11;  // 53 bits
+        p.pos[o * D + d] = __longlong_as_double((long long)bits);
+        int64_t kd;
+        uint32_t fr;
+        fixed_cell((uint64_t)p.vox[v * D + d], bits, p.rho_int[d], p.rho_frac[d], p.level, kd, fr);
+        if (kd >= p.ncell[d]) kd -= p.ncell[d];
+        kd = kd < p.ncell[d] ? kd : p.ncell[d] - 1;
+        p.kc[o * D + d] = (int32_t)kd;
+        p.off[o * D + d] = __fmul_rn(__fmul_rn(__uint2float_rn(fr), 0x1p-32f), p.cf[d]);
+    }
+    p.key[o] = ((uint64_t)w[2 + 2 * D] << 32) | i;
+    p.rad[o] = p.radius;
+    p.cphase[o] = p.phase;
+    p.state[o] = ST_UNDECIDED;
+}
+
+// Dart i of the round (counter (i, round, call) under the run's key), written to candidate slot o.
+__device__ __forceinline__ void dart_body(const DartParams& p, uint32_t i, uint64_t o) {
+    constexpr int WORDS = 2 + 2 * D + 1;
+    constexpr int CALLS = (WORDS + 3) / 4;
+    uint32_t w[CALLS * 4];
+    dart_words<CALLS>(p, i, w);
     const uint64_t r64 = ((uint64_t)w[0] << 32) | w[1];
     const uint64_t v = __umul64hi(r64, p.V);
     if (p.vidx_out) p.vidx_out[o] = v;
@@ -149,10 +222,44 @@ __device__ __forceinline__ void dart_body(const DartParams& p, uint32_t i, uint6
     p.state[o] = ST_UNDECIDED;
 }
 
+// slot t of the round: dart perm[t] in the binned order, else dart t
 __global__ void k_darts(DartParams p) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n) return;
+    dart_body(p, p.perm ? p.perm[t] % p.n : t, t);
+}
+
+__global__ void k_darts32(DartParams p) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.n) return;
+    dart32_body(p, p.perm ? p.perm[t] % p.n : t, t);
+}
+
+// binned order: histogram of the darts' bins, then (after a scan) the permutation
+__global__ void k_dart_bins(DartParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    dart_body(p, i, i);
+    atomicAdd(p.bin_hist + ((p.vbase + dart_voxel(p, i)) >> p.bin_shift), 1u);
+}
+
+__global__ void k_dart_perm(DartParams p) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    place_dart(p, i, i);
+}
+
+// The exact FP64 position of lazy candidate i, by dart_body's own expression (list_of_voxels.ixx:107-129).
+// The empty volatile asm keeps the FP64 work where it is called (the guard band, the survivors).
+__device__ __forceinline__ void lazy_position(const Geo<D>& geo, const CandArgs& c, uint32_t i, double* x) {
+    uint64_t v = (uint64_t)c.cell[i];
+    asm volatile("" : "+l"(v));
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const uint64_t bits = (uint64_t)__double_as_longlong(c.pos[(uint64_t)i * D + d]);
+        const double u = (double)bits * 0x1.0p-53;
+        const double orig = __dadd_rn(geo.inf[d], __dmul_rn((double)c.lvox[v * D + d], c.llen[d]));
+        x[d] = __dadd_rn(orig, __dmul_rn(c.llen[d], u));
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -164,56 +271,83 @@ __global__ void k_darts(DartParams p) {
 template <bool F32>
 __device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, uint32_t i,
                                            uint32_t& rt) {
-    {
-        double x[D];
-#pragma unroll
-        for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
-        const double r = c.rad[i];
-        int32_t k[D];
+    const double r = c.rad[i];
+    int32_t k[D];
+    double x[D];
+    auto fp64_cell = [&]() {
+        // cell and FP32 offsets of an exact FP64 position, as the placed spheres' are formed (k_commit)
         cell_of<D>(g, geo, x, k);
-        bool hit;
-        if constexpr (!F32) {
-            hit = visit_placed<D>(g, geo, k, search_r2(r, g.rmax), [&](int64_t, const double* img, double rs) {
-                return collide64<D>(r, x, rs, img);
-            });
-        } else {
-            // FP32 screen: certain outside the guard band, FP64 retest inside it
-            float offq[D];
+        if (F32) {
 #pragma unroll
             for (int d = 0; d < D; d++) {
                 const double base = __dadd_rn(geo.inf[d], __dmul_rn((double)k[d], g.c[d]));
-                offq[d] = __double2float_rn(__dsub_rn(x[d], base));
-                c.off[(uint64_t)i * D + d] = offq[d];
+                c.off[(uint64_t)i * D + d] = __double2float_rn(__dsub_rn(x[d], base));
                 c.kc[(uint64_t)i * D + d] = k[d];
             }
-            const float rf = __double2float_rn(r);
-            hit = visit_placed_o<D>(g, k, search_r2(r, g.rmax), [&](int64_t idx, const int32_t* o, const int8_t* q) {
-                const float rs = g.mono ? g.rmonof : g.radf[idx];
-                const float R = __fadd_rn(rf, rs);
-                const float R2 = __fmul_rn(R, R);
-                float dlt[D];
-                model_delta<D>(g.cf, o, g.off + idx * D, offq, dlt);
-                const float d2 = sumsq32<D>(dlt);
-                if (d2 < __fsub_rn(R2, g.guard)) return true;
-                if (d2 > __fadd_rn(R2, g.guard)) return false;
-                rt++;
-                double p[D], img[D];
+        }
+    };
+    bool hit;
+    if constexpr (!F32) {
 #pragma unroll
-                for (int d = 0; d < D; d++) p[d] = g.pos[idx * D + d];
-                image_of<D>(geo, p, q, img);
-                return collide64<D>(r, x, g.mono ? g.rmono : g.rad[idx], img);
-            });
+        for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
+        cell_of<D>(g, geo, x, k);
+        hit = visit_placed<D>(g, geo, k, search_r2(r, g.rmax), [&](int64_t, const double* img, double rs) {
+            return collide64<D>(r, x, rs, img);
+        });
+    } else {
+        // FP32 screen: certain outside the guard band, FP64 retest inside it.  A lazy candidate (FP32 darts)
+        // has its cell and offsets already and forms its FP64 position only when a retest or survival needs it.
+        const bool lazy = c.lazy != 0;
+        if (!lazy) {
+#pragma unroll
+            for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
+            fp64_cell();
         }
-        if (hit) {
-            c.state[i] = ST_DEAD;
-            return false;
+        bool have_x = !lazy;
+        float offq[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            k[d] = c.kc[(uint64_t)i * D + d];
+            offq[d] = c.off[(uint64_t)i * D + d];
         }
-        const int64_t idx = cell_index<D>(g, k);
-        c.cell[i] = idx;
-        c.next[i] = atomicExch(c.head + idx, (int32_t)i);
-        atomicOr(c.cocc + (idx >> 5), 1u << (idx & 31));
-        return true;
+        const float rf = __double2float_rn(r);
+        hit = visit_placed_o<D>(g, k, search_r2(r, g.rmax), [&](int64_t idx, const int32_t* o, const int8_t* q) {
+            const float rs = g.mono ? g.rmonof : g.radf[idx];
+            const float R = __fadd_rn(rf, rs);
+            const float R2 = __fmul_rn(R, R);
+            float dlt[D];
+            model_delta<D>(g.cf, o, g.off + idx * D, offq, dlt);
+            const float d2 = sumsq32<D>(dlt);
+            if (d2 < __fsub_rn(R2, g.guard)) return true;
+            if (d2 > __fadd_rn(R2, g.guard)) return false;
+            rt++;
+            if (!have_x) {
+                lazy_position(geo, c, i, x);
+                have_x = true;
+            }
+            double p[D], img[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) p[d] = g.pos[idx * D + d];
+            image_of<D>(geo, p, q, img);
+            return collide64<D>(r, x, g.mono ? g.rmono : g.rad[idx], img);
+        });
+        if (!hit && lazy) {
+            // a survivor: its exact position, and its cell and offsets from it, for the rest of the round
+            if (!have_x) lazy_position(geo, c, i, x);
+#pragma unroll
+            for (int d = 0; d < D; d++) c.pos[(uint64_t)i * D + d] = x[d];
+            fp64_cell();
+        }
     }
+    if (hit) {
+        c.state[i] = ST_DEAD;
+        return false;
+    }
+    const int64_t idx = cell_index<D>(g, k);
+    c.cell[i] = idx;
+    c.next[i] = atomicExch(c.head + idx, (int32_t)i);
+    atomicOr(c.cocc + (idx >> 5), 1u << (idx & 31));
+    return true;
 }
 
 template <bool F32>
@@ -550,8 +684,9 @@ struct RefineParams {
     float lenf[D];
     float nlenf[D];
     float rminf;
-    uint64_t rho_frac[D];  // len / c: 64-bit fraction and integer part (FP32 form's voxel-to-cell map)
+    uint64_t rho_frac[D];  // level-0 voxel length / cell edge: 64-bit fraction and integer part
     uint32_t rho_int[D];
+    int32_t level;         // parent level (fixed-point shift)
 };
 
 // child index with bit d = offset along dimension d, for the child at position t of the corner table
@@ -761,28 +896,28 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
         int32_t k[D];
 #pragma unroll
         for (int d = 0; d < D; d++) {
-            // The voxel centre in cell edges, y = (cc + 1/2) len / c, as the 64-bit fixed-point product
-            // (2 cc + 1) * rho / 2 (rho = len / c, integer part and 64-bit fraction): its integer part is the
-            // cell, its fraction the centre's offset from the cell's corner.  Integer instructions only; the
-            // FP64 pipe of this GPU runs at 1/64 of the FP32 rate.  The error (below 2^-29 cell edges) is
-            // inside the guard band, and only the screen uses these values.
-            const uint64_t m = 2 * (uint64_t)cc[d] + 1;
-            const uint64_t hi = __umul64hi(m, p.rho_frac[d]);
-            const uint64_t lo = m * p.rho_frac[d];
-            const uint64_t two_y = m * (uint64_t)p.rho_int[d] + hi;  // floor(2 y)
-            int64_t kd = (int64_t)(two_y >> 1);
-            const uint32_t fb = ((uint32_t)(two_y & 1u) << 31) | (uint32_t)(lo >> 33);  // frac(y) in 2^-32
+            // The voxel centre in cell edges, y = (cc + 1/2) len / c, in fixed point (fixed_cell): its integer
+            // part is the cell, its fraction the centre's offset from the cell's corner.  Integer instructions
+            // only; the FP64 pipe of this GPU runs at 1/64 of the FP32 rate.  The error (below 2^-31 cell edges)
+            // is far inside the guard band, and only the screen uses these values.
+            int64_t kd;
+            uint32_t fb;
+            fixed_cell((uint64_t)cc[d], 1ull << 52, p.rho_int[d], p.rho_frac[d], p.level, kd, fb);
             if (kd >= g.n[d]) kd -= g.n[d];  // the top face rounds onto the periodic image of cell 0
             k[d] = (int32_t)(kd < g.n[d] ? kd : g.n[d] - 1);
             relc[d] = __fmul_rn(__fmul_rn(__uint2float_rn(fb), 0x1p-32f), g.cf[d]);
             relo[d] = __fsub_rn(relc[d], __fmul_rn(0.5f, p.lenf[d]));
         }
-        // the exact FP64 origin and centre (list_of_voxels.ixx:154-160), for the guard band only
+        // the exact FP64 origin and centre (list_of_voxels.ixx:154-160), for the guard band only.  The empty
+        // volatile asm pins the computation inside the guard-band branch: loop-invariant, it would otherwise be
+        // hoisted onto the common path, where FP64 instructions cost 64 FP32 ones on this GPU.
         auto exact_corners = [&](double* orig, double* centre) {
 #pragma unroll
             for (int d = 0; d < D; d++) {
-                orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cc[d], p.len[d]));
-                centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cc[d], 0.5), p.len[d]));
+                int64_t cv = cc[d];
+                asm volatile("" : "+l"(cv));
+                orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cv, p.len[d]));
+                centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cv, 0.5), p.len[d]));
             }
         };
         float pre0[K_PRE][D], pre1[K_PRE][D], preR2[K_PRE];
@@ -804,7 +939,9 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
             }
         };
         auto exact_R2b = [&](int64_t idx) {
-            const double R = __dadd_rn(g.mono ? g.rmono : g.rad[idx], p.rmin);
+            double rs = g.mono ? g.rmono : g.rad[idx];
+            asm volatile("" : "+d"(rs));  // kept in the guard-band branch (see exact_corners)
+            const double R = __dadd_rn(rs, p.rmin);
             return dbits(__dmul_rn(R, R));
         };
         const float R2q = search_r2(p.rmin, g.rmax);
@@ -1102,7 +1239,7 @@ void op_vox_init(int64_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s) 
 }
 
 void op_darts(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaStream_t s) {
-    DartParams p;
+    DartParams p{};
     p.n = a.n;
     p.V = a.V;
     p.vox = a.vox;
@@ -1122,8 +1259,65 @@ void op_darts(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaStre
     p.cphase = c.phase;
     p.state = c.state;
     p.vidx_out = a.vidx_out;
+    p.perm = a.perm;
     if (a.n == 0) return;
     k_darts<<<nblocks(a.n, 256), 256, 0, s>>>(p);
+    count_launch();
+}
+
+// pass 1 (histogram) when a.bin_off is null, else pass 2 (the permutation a.perm)
+void op_dart_bins(const CandArgs& c, const DartArgs& a, cudaStream_t s) {
+    DartParams p{};
+    p.n = a.n;
+    p.V = a.V;
+    p.seed_lo = (uint32_t)a.seed;
+    p.seed_hi = (uint32_t)(a.seed >> 32);
+    p.round_lo = (uint32_t)a.round;
+    p.round_hi = (uint32_t)(a.round >> 32);
+    p.bin_hist = a.bin_hist;
+    p.bin_off = a.bin_off;
+    p.bin_shift = a.bin_shift;
+    p.vbase = 0;
+    p.perm = a.perm;
+    p.err = c.counters + 2;
+    if (a.n == 0 || !a.bin_hist) return;
+    if (!a.bin_off) k_dart_bins<<<nblocks(a.n, 256), 256, 0, s>>>(p);
+    else k_dart_perm<<<nblocks(a.n, 256), 256, 0, s>>>(p);
+    count_launch();
+}
+
+void op_darts32(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaStream_t s) {
+    DartParams p{};
+    p.n = a.n;
+    p.V = a.V;
+    p.vox = a.vox;
+    for (int d = 0; d < D; d++) {
+        p.len[d] = a.len[d];
+        p.inf[d] = ga.inf[d];
+        p.rho_frac[d] = a.rho_frac[d];
+        p.rho_int[d] = a.rho_int[d];
+        p.ncell[d] = ga.n[d];
+        p.cf[d] = ga.cf[d];
+    }
+    p.seed_lo = (uint32_t)a.seed;
+    p.seed_hi = (uint32_t)(a.seed >> 32);
+    p.round_lo = (uint32_t)a.round;
+    p.round_hi = (uint32_t)(a.round >> 32);
+    p.radius = a.radius;
+    p.phase = a.phase;
+    p.pos = c.pos;
+    p.key = c.key;
+    p.rad = c.rad;
+    p.cphase = c.phase;
+    p.state = c.state;
+    p.vidx_out = nullptr;
+    p.kc = c.kc;
+    p.off = c.off;
+    p.cell = c.cell;
+    p.level = a.level;
+    p.perm = a.perm;
+    if (a.n == 0) return;
+    k_darts32<<<nblocks(a.n, 256), 256, 0, s>>>(p);
     count_launch();
 }
 
@@ -1193,6 +1387,7 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
         p.rho_frac[d] = a.rho_frac[d];
         p.rho_int[d] = a.rho_int[d];
     }
+    p.level = a.level;
     p.rminf = (float)a.rmin;
     return p;
 }
@@ -1236,6 +1431,8 @@ const DimOps kOps = {
     D,
     op_vox_init,
     op_darts,
+    op_darts32,
+    op_dart_bins,
     op_probe,
     op_collect,
     op_settle,
@@ -1253,6 +1450,7 @@ const DimOps kOps = {
     op_batch_table_fill,
     op_b_vox_init,
     op_b_darts,
+    op_b_dart_bins,
     op_b_probe,
     op_b_collect,
     op_b_settle,

@@ -48,15 +48,18 @@ __global__ void k_b_vox_init(BatchArgs b, int64_t* vox) {
     }
 }
 
-// dart t of the round: dart (t - dart_off[s]) of instance s, under the instance's key
+// Slot t of the round holds global dart g = perm[t] (or t): dart (g - dart_off[s]) of instance s, under the
+// instance's key (F32: a lazy candidate).
+template <bool F32>
 __global__ void __launch_bounds__(256) k_b_darts(BatchArgs b, CandArgs c) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= b.ndarts) return;
+    const uint64_t gi = b.perm ? (uint64_t)b.perm[t] % b.ndarts : t;
     const BInst* tab = (const BInst*)b.table;
-    const uint32_t s = segment_of(b.dart_off, b.M, t);
+    const uint32_t s = segment_of(b.dart_off, b.M, gi);
     const BInst& I = tab[s];
     const BatchRound& R = b.rnd[s];
-    DartParams p;
+    DartParams p{};
     p.n = 0;
     p.V = R.V;
     p.vox = b.vox + R.vbase * D;
@@ -77,8 +80,61 @@ __global__ void __launch_bounds__(256) k_b_darts(BatchArgs b, CandArgs c) {
     p.cphase = c.phase;
     p.state = c.state;
     p.vidx_out = nullptr;
-    dart_body(p, (uint32_t)(t - b.dart_off[s]), t);
+    const uint32_t i = (uint32_t)(gi - b.dart_off[s]);
+    if constexpr (F32) {
+        p.kc = c.kc;
+        p.off = c.off;
+        p.cell = c.cell;
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            p.rho_frac[d] = R.rho_frac[d];
+            p.rho_int[d] = R.rho_int[d];
+            p.ncell[d] = I.g.n[d];
+            p.cf[d] = I.g.cf[d];
+        }
+        p.level = R.level;
+        dart32_body(p, i, t);
+    } else {
+        dart_body(p, i, t);
+    }
     b.cinst[t] = s;
+}
+
+// binned dart order over the wave's voxel list: pass 1 (histogram) without bin_off, else pass 2 (perm)
+__global__ void __launch_bounds__(256) k_b_dart_bins(BatchArgs b, CandArgs c) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= b.ndarts) return;
+    const BInst* tab = (const BInst*)b.table;
+    const uint32_t s = segment_of(b.dart_off, b.M, t);
+    const BatchRound& R = b.rnd[s];
+    DartParams p{};
+    p.V = R.V;
+    p.seed_lo = tab[s].seed_lo;
+    p.seed_hi = tab[s].seed_hi;
+    p.round_lo = (uint32_t)b.round;
+    p.round_hi = (uint32_t)(b.round >> 32);
+    p.vbase = R.vbase;
+    p.bin_hist = b.bin_hist;
+    p.bin_off = b.bin_off;
+    p.bin_shift = b.bin_shift;
+    p.perm = b.perm;
+    p.err = c.counters + 2;
+    const uint32_t i = (uint32_t)(t - b.dart_off[s]);
+    if (!b.bin_off) atomicAdd(b.bin_hist + ((R.vbase + dart_voxel(p, i)) >> b.bin_shift), 1u);
+    else place_dart(p, i, (uint32_t)t);
+}
+
+// the candidate arguments seen by one candidate of instance s: its cell lists, and for a lazy candidate
+// the voxel segment and length its exact position comes from
+__device__ __forceinline__ CandArgs with_instance(const CandArgs& c, const BatchArgs& b, const BInst& I, uint32_t s) {
+    CandArgs ci = with_lists(c, I);
+    if (c.lazy) {
+        const BatchRound& R = b.rnd[s];
+        ci.lvox = b.vox + R.vbase * D;
+#pragma unroll
+        for (int d = 0; d < D; d++) ci.llen[d] = R.len[d];
+    }
+    return ci;
 }
 
 template <bool F32>
@@ -87,10 +143,11 @@ __global__ void __launch_bounds__(512, 2) k_b_probe(BatchArgs b, CandArgs c) {
     uint32_t rt = 0;
     bool alive = false;
     if (i < c.n && c.state[i] == ST_UNDECIDED) {
-        const BInst& I = ((const BInst*)b.table)[b.cinst[i]];
+        const uint32_t s = b.cinst[i];
+        const BInst& I = ((const BInst*)b.table)[s];
         const Grid<D> g = I.g;
         const Geo<D> geo = I.geo;
-        alive = probe_body<F32>(g, geo, with_lists(c, I), i, rt);
+        alive = probe_body<F32>(g, geo, with_instance(c, b, I, s), i, rt);
     }
     const uint32_t slot = warp_append(&c.counters[0], alive);
     if (alive) c.alive[slot] = i;
@@ -204,6 +261,7 @@ __global__ void __launch_bounds__(512, 2) k_b_refine_mask(BatchArgs b, RefineArg
                 p.rho_frac[d] = R.rho_frac[d];
                 p.rho_int[d] = R.rho_int[d];
             }
+            p.level = R.level;
             p.rmin = g.rmono;
             p.rminf = (float)g.rmono;
             p.masks = nullptr;
@@ -373,9 +431,16 @@ void op_b_vox_init(const BatchArgs& b, int64_t* vox, cudaStream_t s) {
     count_launch();
 }
 
-void op_b_darts(const BatchArgs& b, const CandArgs& c, cudaStream_t s) {
+void op_b_darts(const BatchArgs& b, const CandArgs& c, int f32, cudaStream_t s) {
     if (b.ndarts == 0) return;
-    k_b_darts<<<nblocks(b.ndarts, 256), 256, 0, s>>>(b, c);
+    if (f32) k_b_darts<true><<<nblocks(b.ndarts, 256), 256, 0, s>>>(b, c);
+    else k_b_darts<false><<<nblocks(b.ndarts, 256), 256, 0, s>>>(b, c);
+    count_launch();
+}
+
+void op_b_dart_bins(const BatchArgs& b, const CandArgs& c, cudaStream_t s) {
+    if (b.ndarts == 0 || !b.bin_hist) return;
+    k_b_dart_bins<<<nblocks(b.ndarts, 256), 256, 0, s>>>(b, c);
     count_launch();
 }
 

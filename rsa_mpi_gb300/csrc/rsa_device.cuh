@@ -27,6 +27,7 @@ enum : uint32_t {
     ERR_BLOCKER_OVERFLOW = 2u,   // (informational) a candidate had more than NB lower colliders
     ERR_PREFILTER_OVERFLOW = 4u, // (informational) a parent voxel had more than K prefilter spheres
     ERR_WRITE_BOUNDS = 8u,       // a refinement output offset beyond the output buffer (write skipped)
+    ERR_DART_SLOT = 16u,         // a dart found its bin of the binned order full (dart skipped)
 };
 
 constexpr int NB = 24;     // stored lower-priority colliders per candidate (more: rescan)
@@ -194,7 +195,13 @@ __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, 
         const float rest = rows_r2[r];
         if (rest > R2q) break;
         const int8_t* row = rows + r * (D + 1);
-        const int32_t o0max = 1 + (int32_t)(sqrtf(R2q - rest) / c0f);
+        // o0max = 1 + floor(sqrt(R2q - rest) / c0) without a square root or a division: the largest j with
+        // j^2 c0^2 <= R2q - rest, counted up to the row's own extent (R2q carries a 1e-4 margin, far above the
+        // float rounding of either form)
+        const float avail = R2q - rest, c0sq = c0f * c0f;
+        const int32_t ext = 1 + max(-(int32_t)row[0], (int32_t)row[1]);
+        int32_t o0max = 1;
+        while (o0max < ext && __fmul_rn((float)(o0max * o0max), c0sq) <= avail) o0max++;
         int8_t q[D];
         int64_t base = 0;
 #pragma unroll
@@ -285,6 +292,29 @@ __device__ __forceinline__ float sumsq32(const float* v) {
 #pragma unroll
     for (int d = 0; d < D; d++) s = __fadd_rn(s, __fmul_rn(v[d], v[d]));
     return s;
+}
+
+// Fixed-point cell map of the FP32 form: y = (a + bits 2^-53) (ri + rf 2^-64) 2^-shift for integers a >= 0,
+// bits < 2^53 and 0 <= shift < 64.  k = floor(y); frac32 = the top 32 bits of y's fraction.  Integer
+// instructions only; exact but for the truncation of rf (below a 2^-64 cell edge per unit of a 2^-shift).
+__device__ __forceinline__ void fixed_cell(uint64_t a, uint64_t bits, uint32_t ri, uint64_t rf, int shift, int64_t& k,
+                                           uint32_t& frac32) {
+    const uint64_t lo1 = a * rf, hi1 = __umul64hi(a, rf);
+    const uint64_t iu = bits * (uint64_t)ri;                 // u ri in 2^-53 units
+    const uint64_t f2 = (iu & ((1ull << 53) - 1)) << 11;     // its fraction, 2^-64 units
+    const uint64_t f3 = __umul64hi(bits << 11, rf);          // u rf, 2^-64 units
+    uint64_t lo = lo1 + f2;
+    uint64_t carry = lo < f2 ? 1u : 0u;
+    lo += f3;
+    carry += lo < f3 ? 1u : 0u;
+    const uint64_t ip = a * (uint64_t)ri + hi1 + (iu >> 53) + carry;
+    if (shift == 0) {
+        k = (int64_t)ip;
+        frac32 = (uint32_t)(lo >> 32);
+    } else {
+        k = (int64_t)(ip >> shift);
+        frac32 = (uint32_t)(((lo >> shift) | (ip << (64 - shift))) >> 32);
+    }
 }
 
 // squared search radius (r_query + r_max)^2 with a margin, as float

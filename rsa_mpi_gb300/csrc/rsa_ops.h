@@ -55,6 +55,11 @@ struct CandArgs {
     uint8_t* nblk;
     uint32_t* und;      // undecided count after each settle iteration (und[0] after collect)
     uint64_t* gather;   // keys of accepted candidates (count cap)
+    // lazy candidates (FP32-form darts): until the probe forms the exact position, cell holds the dart's
+    // voxel and pos its 53 random bits per coordinate; lvox and llen are that round's voxel list and length
+    int32_t lazy;
+    const int64_t* lvox;
+    double llen[MAX_D];
 };
 
 struct DartArgs {
@@ -67,6 +72,15 @@ struct DartArgs {
     double radius;
     int32_t phase;
     uint64_t* vidx_out;  // optional: chosen voxel per dart
+    uint64_t rho_frac[MAX_D];  // FP32-form darts: level-0 voxel length / cell edge (voxel_cell_ratio)
+    uint32_t rho_int[MAX_D];
+    int32_t level;             // voxel level (the fixed-point shift)
+    // binned order (optional): slot t of the round holds dart perm[t]; DimOps::dart_bins builds perm, the darts
+    // of each bin of 2^bin_shift consecutive voxels together
+    uint32_t* bin_hist;        // per bin: dart count (pass 1; consumed by pass 2)
+    const uint64_t* bin_off;   // per bin: first slot (exclusive scan of the counts; null in pass 1)
+    int32_t bin_shift;
+    uint32_t* perm;            // n dart indices
 };
 
 struct RefineArgs {
@@ -84,17 +98,21 @@ struct RefineArgs {
     uint32_t* survivors;  // parents not covered (remove_covered keeps them)
     unsigned long long* visits;  // occupied stencil cells visited by the mask pass
     unsigned long long* retests; // (voxel, sphere) pairs redone in FP64 (guard-band form)
-    uint64_t rho_frac[MAX_D];    // len / c in 64-bit fixed point (voxel_cell_ratio)
+    uint64_t rho_frac[MAX_D];    // level-0 voxel length / cell edge in fixed point (voxel_cell_ratio)
     uint32_t rho_int[MAX_D];
+    int32_t level;               // parent level (the fixed-point shift)
 };
 
-// len / c (voxel length in cell edges) as an integer part and a 64-bit fraction, for the FP32 form's
-// fixed-point map from voxel coordinates to cells
-inline void voxel_cell_ratio(double len, double c, uint32_t* rho_int, uint64_t* rho_frac) {
-    const double rho = len / c;
+// The FP32 form maps a point of a voxel at level `level` to cells in 64-bit fixed point:
+// y = (coordinate + u) * rho0 * 2^-level cell edges, rho0 = len0 / c (level-0 voxel length over cell edge; the
+// voxel length halves exactly per level), held as an integer part and a 64-bit fraction with the double's full
+// precision.  len is the current length; returns false when y * 2^level could leave 64 bits.
+inline bool voxel_cell_ratio(double len, int level, double c, int32_t n, uint32_t* rho_int, uint64_t* rho_frac) {
+    const double rho = std::ldexp(len, level) / c;
     const double ip = std::floor(rho);
     *rho_int = (uint32_t)ip;
     *rho_frac = (uint64_t)std::ldexp(rho - ip, 64);  // rho - ip <= 1 - 2^-53: below 2^64
+    return std::ldexp((double)n * (ip + 1), level + 1) < 9.0e18;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -115,8 +133,9 @@ struct BatchRound {      // per instance, per round
     uint64_t V;          // voxels in its segment
     double len[MAX_D];   // voxel length at its level
     double nlen[MAX_D];  // child length = 0.5 * len
-    uint64_t rho_frac[MAX_D];  // len / c (voxel_cell_ratio)
+    uint64_t rho_frac[MAX_D];  // level-0 voxel length / cell edge (voxel_cell_ratio)
     uint32_t rho_int[MAX_D];
+    int32_t level;             // its voxel level
     int32_t refine;      // subdivide its voxels after this round's pass
 };
 
@@ -131,6 +150,10 @@ struct BatchArgs {
     uint32_t* cinst;           // instance of each candidate
     uint32_t* acc;             // spheres accepted per instance in the current round
     uint64_t round;            // round index (the Philox counter's round words)
+    uint32_t* bin_hist;        // binned dart order over the wave's voxel list (see DartArgs), or null
+    const uint64_t* bin_off;   // null in pass 1
+    int32_t bin_shift;
+    uint32_t* perm;            // slot t holds global dart perm[t]
     uint64_t ndarts;           // darts of the round, all instances
     uint64_t V;                // voxels, all instances
     uint64_t nwords;           // occupancy words, all instances
@@ -142,6 +165,8 @@ struct DimOps {
     int D;
     void (*vox_init)(int64_t* vox, uint64_t V, const int64_t* nvox, cudaStream_t s);
     void (*darts)(const GridArgs& g, const CandArgs& c, const DartArgs& a, cudaStream_t s);
+    void (*darts32)(const GridArgs& g, const CandArgs& c, const DartArgs& a, cudaStream_t s);  // lazy candidates
+    void (*dart_bins)(const CandArgs& c, const DartArgs& a, cudaStream_t s);  // binned order: pass 1 or 2
     void (*probe)(const GridArgs& g, const CandArgs& c, int f32, cudaStream_t s);
     void (*collect)(const GridArgs& g, const CandArgs& c, int f32, cudaStream_t s);
     void (*settle)(const GridArgs& g, const CandArgs& c, int iteration, int f32, cudaStream_t s);
@@ -161,7 +186,8 @@ struct DimOps {
     // copies the instance table to the device (synchronous); returns a cudaError_t
     int (*batch_table_fill)(const BatchInstance* inst, uint32_t M, void* d_table, cudaStream_t s);
     void (*b_vox_init)(const BatchArgs& b, int64_t* vox, cudaStream_t s);
-    void (*b_darts)(const BatchArgs& b, const CandArgs& c, cudaStream_t s);
+    void (*b_darts)(const BatchArgs& b, const CandArgs& c, int f32, cudaStream_t s);  // f32: lazy candidates
+    void (*b_dart_bins)(const BatchArgs& b, const CandArgs& c, cudaStream_t s);  // pass 1 or 2 (as dart_bins)
     void (*b_probe)(const BatchArgs& b, const CandArgs& c, int f32, int block, cudaStream_t s);
     void (*b_collect)(const BatchArgs& b, const CandArgs& c, int f32, int block, cudaStream_t s);
     void (*b_settle)(const BatchArgs& b, const CandArgs& c, int iteration, int f32, int block, cudaStream_t s);

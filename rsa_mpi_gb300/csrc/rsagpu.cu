@@ -133,6 +133,11 @@ struct rsagpu_algo {
     int level = 0;
     int64_t nvox0[MAX_D]{};
     double len[MAX_D]{};
+    uint32_t* bin_hist = nullptr;  // binned dart order: per-bin counts and first slots, the permutation
+    uint64_t* bin_off = nullptr;
+    uint64_t bins_cap = 0;
+    uint32_t* perm = nullptr;
+    uint64_t perm_cap = 0;
     uint32_t* masks = nullptr;
     uint64_t masks_cap = 0;
     uint32_t* block_counts = nullptr;
@@ -163,6 +168,7 @@ struct rsagpu_algo {
     // state
     bool begun = false;
     bool heads_dirty = false;  // a round stopped before its commit cleared the candidate lists
+    bool lazy = false;         // the candidates in the buffers came from the FP32-form darts
     uint64_t seed = 0, round = 0;
     std::vector<TraceRow> trace;
     rsagpu_stats stats{};
@@ -172,6 +178,9 @@ struct rsagpu_algo {
         cand.release();
         dfree(vox[0]);
         dfree(vox[1]);
+        dfree(bin_hist);
+        dfree(bin_off);
+        dfree(perm);
         dfree(masks);
         dfree(block_counts);
         dfree(block_offsets);
@@ -302,8 +311,9 @@ GridPlan plan_grid(int D, const double* inf, const double* L, double rmin, doubl
         // errs by at most E (float rounding of c, of the offsets, of the product and of the two sums, and of
         // a voxel length); every difference is below A; the squares and the D-term sum add (D+1) roundings of
         // a quantity below D A^2; the threshold (r_s + r_q)^2 in float adds 8 ulps of (2 r_max)^2.  The voxel
-        // offsets of the mask pass come from a fixed-point cell map (error below 2^-29 c) and two more float
-        // roundings (the centre's offset, then the origin's = centre's - len / 2): u (4 c + 2 len) more.
+        // offsets of the mask pass come from a fixed-point cell map (error below 2^-31 c) and two more float
+        // roundings (the centre's offset, then the origin's = centre's - len / 2): u (4 c + 2 len) more; the
+        // FP32-form darts' offsets come from the same kind of map and are covered by the same term.
         const double u = std::ldexp(1.0, -24);
         double cmax = 0;
         int wmax = 0;
@@ -406,6 +416,9 @@ CandArgs cand_args(rsagpu_algo* A, uint32_t n) {
     c.head = A->dom->grid.head;
     c.cocc = A->dom->grid.cocc;
     c.und = c.counters + COUNTERS;
+    c.lazy = A->lazy ? 1 : 0;
+    c.lvox = A->vox[A->cur];
+    for (int d = 0; d < A->dom->dim; d++) c.llen[d] = A->len[d];
     return c;
 }
 
@@ -480,8 +493,11 @@ void refine(rsagpu_algo* A) {
     for (int d = 0; d < D; d++) {
         r.len[d] = A->len[d];
         r.nlen[d] = 0.5 * A->len[d];
-        voxel_cell_ratio(A->len[d], A->dom->grid.a.c[d], &r.rho_int[d], &r.rho_frac[d]);
+        if (!voxel_cell_ratio(A->len[d], A->level, A->dom->grid.a.c[d], A->dom->grid.a.n[d], &r.rho_int[d],
+                              &r.rho_frac[d]))
+            raise(RSAGPU_ERR_CAPACITY, "level %d too deep for the fixed-point cell map", A->level);
     }
+    r.level = A->level;
     r.rmin = A->rg.rmin();
     r.masks = A->masks;
     r.warp_counts = A->block_counts;
@@ -689,6 +705,7 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
     if (n_greedy) *n_greedy = may_outreach ? greedy : A->h_counters[1];
     if (A->h_counters[2] & ERR_DOUBLE_OCCUPANCY)
         raise(RSAGPU_ERR_INVARIANT, "two accepted centres in one grid cell");
+    if (A->h_counters[2] & ERR_DART_SLOT) raise(RSAGPU_ERR_INVARIANT, "binned dart order: a bin overflowed");
     (void)keep_state;
     A->placed += A->h_counters[1];
     if (A->timing) A->stats.ms_commit += ev_ms(A, 4, 5);
@@ -845,7 +862,44 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         const auto tp0 = std::chrono::steady_clock::now();
         ev_record(A, 0);
         CandArgs c = cand_args(A, (uint32_t)C);
-        A->ops->darts(dom->grid.a, c, da, A->stream);
+        {
+            // binned order: slot t of the round holds dart perm[t], the darts of each voxel region together
+            da.bin_shift = dart_bin_shift(A->V, C);
+            const uint64_t nbins = ((A->V - 1) >> da.bin_shift) + 1;
+            if (nbins > A->bins_cap) {
+                dfree(A->bin_hist);
+                dfree(A->bin_off);
+                A->bins_cap = std::max<uint64_t>(nbins, A->bins_cap + A->bins_cap / 2);
+                A->bin_hist = dalloc<uint32_t>(A->bins_cap);
+                A->bin_off = dalloc<uint64_t>(A->bins_cap + 1);
+            }
+            if (C > A->perm_cap) {
+                dfree(A->perm);
+                A->perm_cap = std::max<uint64_t>(C, A->perm_cap + A->perm_cap / 2);
+                A->perm = dalloc<uint32_t>(A->perm_cap);
+            }
+            CK(cudaMemsetAsync(A->bin_hist, 0, nbins * sizeof(uint32_t), A->stream));
+            da.bin_hist = A->bin_hist;
+            da.perm = A->perm;
+            A->ops->dart_bins(c, da, A->stream);  // histogram
+            launch_scan_blocks(A->bin_hist, A->bin_off, nbins, nullptr, A->stream);
+            da.bin_off = A->bin_off;
+            A->ops->dart_bins(c, da, A->stream);  // permutation
+        }
+        if (A->form == RSAGPU_FORM_FP32_GUARD) {
+            // FP32 form: lazy candidates (cell and offsets in fixed point, the FP64 position formed in the
+            // probe for the candidates that need it)
+            for (int d = 0; d < D; d++)
+                if (!voxel_cell_ratio(A->len[d], A->level, dom->grid.a.c[d], dom->grid.a.n[d], &da.rho_int[d],
+                                      &da.rho_frac[d]))
+                    raise(RSAGPU_ERR_CAPACITY, "level %d too deep for the fixed-point cell map", A->level);
+            da.level = A->level;
+            A->ops->darts32(dom->grid.a, c, da, A->stream);
+            A->lazy = true;
+        } else {
+            A->ops->darts(dom->grid.a, c, da, A->stream);
+            A->lazy = false;
+        }
         ev_record(A, 1);
         uint64_t n_hits = 0;
         const uint64_t n_new = decide_round(A, (uint32_t)C, remaining, may, false, &n_hits);
@@ -1308,6 +1362,7 @@ int rsagpu_algo_replay_round(rsagpu_algo* algo, uint64_t n, const double* pos, c
         if (phase) CK(cudaMemcpyAsync(c.phase, phase, n * sizeof(int32_t), cudaMemcpyHostToDevice, algo->stream));
         else CK(cudaMemsetAsync(c.phase, 0, n * sizeof(int32_t), algo->stream));
         CK(cudaMemsetAsync(c.state, ST_UNDECIDED, n, algo->stream));
+        algo->lazy = false;  // exact positions given
         *n_new = decide_round(algo, (uint32_t)n, max_new, may_outreach != 0, true);
         std::vector<uint8_t> st(n);
         CK(cudaMemcpyAsync(st.data(), c.state, n, cudaMemcpyDeviceToHost, algo->stream));
@@ -1381,6 +1436,7 @@ int rsagpu_algo_draw_darts(rsagpu_algo* algo, uint64_t seed, uint64_t round, uin
         da.vidx_out = algo->cand.vidx;
         CandArgs c = cand_args(algo, (uint32_t)n);
         algo->ops->darts(algo->dom->grid.a, c, da, algo->stream);
+        algo->lazy = false;
         if (pos) CK(cudaMemcpyAsync(pos, c.pos, n * D * sizeof(double), cudaMemcpyDeviceToHost, algo->stream));
         if (key) CK(cudaMemcpyAsync(key, c.key, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, algo->stream));
         if (voxel_index)
