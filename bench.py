@@ -105,6 +105,7 @@ class ClockSampler:
 
 
 FORM_NAMES = {0: "plain FP64", 1: "FP32 screen + FP64 guard-band retest"}
+FORM_KERNEL = {0: "k_refine_mask", 1: "k_refine_mask32"}
 
 
 def run_gpu_step(dim, L, r, seed, form=1):
@@ -115,11 +116,11 @@ def run_gpu_step(dim, L, r, seed, form=1):
     algo.set_form(form)
     algo.proceed(seed)
     st = algo.stats()
-    ms, by = algo.kernel_profile()
+    ms, by, vx = algo.kernel_profile()
     n = dom.count()
     algo.close()
     dom.close()
-    return n, st, ms, by
+    return n, st, ms, by, vx
 
 
 def run_e2e_step(dim, L, r, seed, form=1):
@@ -342,16 +343,17 @@ def main():
     launches0 = kernel_launches()
     barrier()
     spheres, dev_ms, wall = 0, 0.0, 0.0
-    mask_ms, mask_bytes = [], []
+    mask_ms, mask_bytes, mask_vox = [], [], []
     stats = None
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            n, st, ms, by = run_gpu_step(dim, L, r, seed, args.form)
+            n, st, ms, by, vx = run_gpu_step(dim, L, r, seed, args.form)
             spheres += n
             dev_ms += st["ms_total"]
             mask_ms += list(ms)
             mask_bytes += list(by)
+            mask_vox += list(vx)
             stats = st
         barrier()
         wall = time.perf_counter() - t0
@@ -363,7 +365,7 @@ def main():
         primary = {"spheres_per_s": spheres / (dev_ms * 1e-3), "ms": dev_ms / args.steps, "retests": stats["retests"]}
         forms[FORM_NAMES[args.form]] = primary
         other = 1 - args.form
-        n2, st2, _, _ = run_gpu_step(dim, L, r, seed, other)
+        n2, st2, _, _, _ = run_gpu_step(dim, L, r, seed, other)
         forms[FORM_NAMES[other]] = {"spheres_per_s": n2 / (st2["ms_total"] * 1e-3), "ms": st2["ms_total"],
                                     "retests": st2["retests"], "same_spheres": n2 == spheres // max(1, args.steps)}
         base = forms[FORM_NAMES[0]]["spheres_per_s"]
@@ -407,13 +409,15 @@ def main():
     mm = np.asarray(mask_ms)
     mb = np.asarray(mask_bytes)
     achieved = float(mb.sum() / (mm.sum() * 1e-3) / 1e9) if mm.sum() > 0 else 0.0
+    # DRAM traffic per launch: bytes per parent voxel measured by ncu (dram__bytes_read.sum +
+    # dram__bytes_write.sum) on a smaller case of the same kernel, times this workload's voxels per launch
     traffic_path = os.path.join(ROOT, "profiles", "refine_mask_traffic.json")
-    traffic = None
-    if os.path.exists(traffic_path):
-        try:
-            traffic = json.load(open(traffic_path)).get("bytes_per_launch")
-        except Exception:
-            traffic = None
+    traffic, traffic_note = None, None
+    if os.path.exists(traffic_path) and len(mask_vox):
+        tj = json.load(open(traffic_path)).get(FORM_KERNEL[args.form], {})
+        if tj.get("bytes_per_voxel"):
+            traffic = float(tj["bytes_per_voxel"]) * float(np.mean(mask_vox))
+            traffic_note = tj.get("note")
     line = {
         "metric": METRIC,
         "value": spheres_all / (dev_ms_max * 1e-3),
@@ -430,8 +434,9 @@ def main():
         "config": {"workload": desc, "form": FORM_NAMES[args.form], "spheres_per_step": spheres // max(1, args.steps),
                    "parallelism": f"replicas x{world}", "l2": "working set > L2 (no flush needed)"},
         "wall_ms_per_step": wall_max * 1e3 / args.steps,
-        "roofline": {"bound": "hbm", "kernel": "k_refine_mask32" if args.form == 1 else "k_refine_mask", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+        "roofline": {"bound": "hbm", "kernel": FORM_KERNEL[args.form], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic, "traffic_note": traffic_note,
+                     "voxels_per_launch": float(np.mean(mask_vox)) if len(mask_vox) else 0.0,
                      "share_of_step": float(mm.sum() / max(dev_ms, 1e-9)),
                      "launches": int(len(mm)), "algorithmic_bytes_per_launch": float(mb.mean()) if len(mb) else 0.0},
         "e2e": {"value": e2e_all / e2e_max, "unit": "spheres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(d2h)},

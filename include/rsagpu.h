@@ -135,7 +135,8 @@ int rsagpu_algo_stats(rsagpu_algo* algo, rsagpu_stats* out);
 /* Per launch of the refinement's mask kernel in the last proceed(): device milliseconds (CUDA events
  * on the algo's stream around the launch) and algorithmic bytes (parent coordinates, stencil occupancy
  * bits up to the grid size, visited spheres up to the spheres placed, child masks). */
-int rsagpu_algo_kernel_profile(rsagpu_algo* algo, double* ms, double* bytes, uint64_t cap, uint64_t* n_out);
+int rsagpu_algo_kernel_profile(rsagpu_algo* algo, double* ms, double* bytes, double* voxels, uint64_t cap,
+                               uint64_t* n_out);
 /* Learned schedule training data: after each pass the schedule's decision is flipped with probability
  * epsilon (host RNG seeded with seed).  0 = off (default). */
 int rsagpu_algo_set_exploration(rsagpu_algo* algo, double epsilon, uint64_t seed);

@@ -93,7 +93,7 @@ _SIGS = {
     "rsagpu_algo_trace": (C.c_int, [_vp, _u64, _u64, _u64, _u8, C.POINTER(C.c_int32), C.c_uint64, _u64]),
     "rsagpu_algo_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "rsagpu_algo_set_timing": (C.c_int, [_vp, C.c_int]),
-    "rsagpu_algo_kernel_profile": (C.c_int, [_vp, _d, _d, C.c_uint64, _u64]),
+    "rsagpu_algo_kernel_profile": (C.c_int, [_vp, _d, _d, _d, C.c_uint64, _u64]),
     "rsagpu_algo_set_exploration": (C.c_int, [_vp, C.c_double, C.c_uint64]),
     "rsagpu_algo_trace_features": (C.c_int, [_vp, _f32, _u8, _d, _d, C.c_uint64, _u64]),
     "rsagpu_algo_begin": (C.c_int, [_vp]),

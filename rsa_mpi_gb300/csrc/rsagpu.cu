@@ -146,7 +146,7 @@ struct rsagpu_algo {
     uint32_t* d_err = nullptr;
     unsigned long long* d_visits = nullptr;
     uint64_t placed = 0;              // spheres in the grid
-    std::vector<double> mask_ms, mask_bytes;  // per refine_mask launch
+    std::vector<double> mask_ms, mask_bytes, mask_voxels;  // per refine_mask launch
     // candidates
     CandBuffers cand;
     uint32_t* h_counters = nullptr;  // pinned mirror: COUNTERS + MAX_SETTLE + 1
@@ -473,6 +473,7 @@ void begin(rsagpu_algo* A) {
     A->stats.peak_voxels = V;
     A->mask_ms.clear();
     A->mask_bytes.clear();
+    A->mask_voxels.clear();
     A->passes_at_level = 0;
     A->prev_miss = 1.0;
     A->level_start_V = V;
@@ -534,6 +535,7 @@ void refine(rsagpu_algo* A) {
         // bytes per visited sphere: FP64 centre + radius, or FP32 offsets (+ FP32 radius unless one class)
         const double per_sphere = A->form == RSAGPU_FORM_FP32_GUARD ? 4.0 * D + (g.mono ? 0 : 4) : 8.0 * D + (g.mono ? 0 : 8);
         A->mask_ms.push_back(ms);
+        A->mask_voxels.push_back((double)A->V);
         A->mask_bytes.push_back((double)A->V * 8 * D + bits / 8 + sph * per_sphere + (double)A->V * 4 * A->ops->mask_words);
     }
     if (survivors == 0) {
@@ -1247,12 +1249,14 @@ int rsagpu_algo_set_mlp(rsagpu_algo* algo, const uint16_t* w, uint64_t n) {
     });
 }
 
-int rsagpu_algo_kernel_profile(rsagpu_algo* algo, double* ms, double* bytes, uint64_t cap, uint64_t* n_out) {
+int rsagpu_algo_kernel_profile(rsagpu_algo* algo, double* ms, double* bytes, double* voxels, uint64_t cap,
+                               uint64_t* n_out) {
     if (!algo || !n_out) return fail(RSAGPU_ERR_ARG, "null argument");
     *n_out = algo->mask_ms.size();
     for (uint64_t i = 0; i < std::min<uint64_t>(cap, algo->mask_ms.size()); i++) {
         if (ms) ms[i] = algo->mask_ms[i];
         if (bytes) bytes[i] = algo->mask_bytes[i];
+        if (voxels) voxels[i] = algo->mask_voxels[i];
     }
     return RSAGPU_OK;
 }

@@ -156,14 +156,16 @@ class Algo:
         check(lib().rsagpu_algo_set_timing(self._h, 1 if on else 0))
 
     def kernel_profile(self):
-        """(ms, algorithmic bytes) per refine-mask launch of the last proceed()."""
+        """(ms, algorithmic bytes, parent voxels) per refine-mask launch of the last proceed()."""
         n = C.c_uint64()
-        check(lib().rsagpu_algo_kernel_profile(self._h, None, None, 0, C.byref(n)))
+        check(lib().rsagpu_algo_kernel_profile(self._h, None, None, None, 0, C.byref(n)))
         k = n.value
         ms = np.zeros(max(k, 1))
         by = np.zeros(max(k, 1))
-        check(lib().rsagpu_algo_kernel_profile(self._h, ptr(ms, _lib._d), ptr(by, _lib._d), k, C.byref(n)))
-        return ms[:k], by[:k]
+        vx = np.zeros(max(k, 1))
+        check(lib().rsagpu_algo_kernel_profile(self._h, ptr(ms, _lib._d), ptr(by, _lib._d), ptr(vx, _lib._d), k,
+                                               C.byref(n)))
+        return ms[:k], by[:k], vx[:k]
 
     def proceed(self, seed: int):
         check(lib().rsagpu_algo_proceed(self._h, int(seed)))
