@@ -382,8 +382,8 @@ def main():
                                            "heuristic_rounds": h4[1]["rounds"], "learned_rounds": l4[1]["rounds"],
                                            "heuristic_spheres": h4[0], "learned_spheres": l4[0]}
         forms["learned schedule (FP32 form)"] = learned
-        forms["batched (config 4)"] = batched_form()
         forms["FP32 guard band, polydisperse (config 3)"] = precision_form()
+        forms["batched (config 4)"] = batched_form()
 
     # e2e through the C ABI with host buffers
     e2e_n, e2e_s, d2h = 0, 0.0, 0

@@ -55,6 +55,7 @@ __host__ __device__ inline Grid<D> make_grid(const GridArgs& a) {
     g.R = a.R;
     g.rows_r2 = a.rows_r2;
     g.c0f = (float)(1.0 / a.inv_c[0]);
+    g.inv_c0f = (float)a.inv_c[0];
     g.rmax = a.rmax;
     g.off = a.off;
     g.radf = a.radf;
@@ -291,7 +292,7 @@ __device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, 
 #pragma unroll
         for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
         cell_of<D>(g, geo, x, k);
-        hit = visit_placed<D>(g, geo, k, search_r2(r, g.rmax), [&](int64_t, const double* img, double rs) {
+        hit = visit_placed<D>(g, geo, k, nullptr, search_r2(r, g.rmax), [&](int64_t, const double* img, double rs) {
             return collide64<D>(r, x, rs, img);
         });
     } else {
@@ -311,7 +312,7 @@ __device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, 
             offq[d] = c.off[(uint64_t)i * D + d];
         }
         const float rf = __double2float_rn(r);
-        hit = visit_placed_o<D>(g, k, search_r2(r, g.rmax), [&](int64_t idx, const int32_t* o, const int8_t* q) {
+        hit = visit_placed_o<D>(g, k, offq, search_r2(r, g.rmax), [&](int64_t idx, const int32_t* o, const int8_t* q) {
             const float rs = g.mono ? g.rmonof : g.radf[idx];
             const float R = __fadd_rn(rf, rs);
             const float R2 = __fmul_rn(R, R);
@@ -367,8 +368,8 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
 // Visits the same-round candidates in the stencil around cell k (linked lists head/next).
 template <class F>
 __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c,
-                                                 const int32_t* k, float R2q, F&& f) {
-    walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.c0f, R2q, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
+                                                 const int32_t* k, const float* qo, float R2q, F&& f) {
+    walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.cf, g.inv_c0f, R2q, k, qo, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
         for (int32_t x = lo; x <= hi; x += 32) {
             const int len = hi - x + 1 < 32 ? hi - x + 1 : 32;
             uint32_t bits = occ_bits(c.cocc, base + x, len);  // cells holding a candidate of this round
@@ -390,9 +391,9 @@ __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>&
 
 // Same walk with the integer cell offset o of each candidate (FP32 screen); f(j, o, q).
 template <class F>
-__device__ __forceinline__ void visit_candidates_o(const Grid<D>& g, const CandArgs& c, const int32_t* k, float R2q,
-                                                   F&& f) {
-    walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.c0f, R2q, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
+__device__ __forceinline__ void visit_candidates_o(const Grid<D>& g, const CandArgs& c, const int32_t* k, const float* qo,
+                                                   float R2q, F&& f) {
+    walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.cf, g.inv_c0f, R2q, k, qo, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
         int32_t o[D];
 #pragma unroll
         for (int d = 1; d < D; d++) o[d] = row[1 + d];
@@ -469,7 +470,7 @@ __device__ __forceinline__ bool collect_body(const Grid<D>& g, const Geo<D>& geo
         if constexpr (!F32) {
             int32_t k[D];
             cell_of<D>(g, geo, x, k);
-            visit_candidates(g, geo, c, k, search_r2(r, g.rmax), [&](int32_t j, const double* img) {
+            visit_candidates(g, geo, c, k, nullptr, search_r2(r, g.rmax), [&](int32_t j, const double* img) {
                 if (!precedes(c.key[j], j, key, i)) return false;
                 if (collide64<D>(r, x, c.rad[j], img)) record(j);
                 return false;
@@ -483,7 +484,7 @@ __device__ __forceinline__ bool collect_body(const Grid<D>& g, const Geo<D>& geo
                 offq[d] = c.off[(uint64_t)i * D + d];
             }
             const float rf = __double2float_rn(r);
-            visit_candidates_o(g, c, k, search_r2(r, g.rmax), [&](int32_t j, const int32_t* o, const int8_t* q) {
+            visit_candidates_o(g, c, k, offq, search_r2(r, g.rmax), [&](int32_t j, const int32_t* o, const int8_t* q) {
                 if (!precedes(c.key[j], j, key, i)) return false;
                 if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) record(j);
                 return false;
@@ -539,7 +540,7 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
                     if constexpr (!F32) {
                         int32_t k[D];
                         cell_of<D>(g, geo, x, k);
-                        visit_candidates(g, geo, c, k, search_r2(r, g.rmax), [&](int32_t j, const double* img) {
+                        visit_candidates(g, geo, c, k, nullptr, search_r2(r, g.rmax), [&](int32_t j, const double* img) {
                             if (!precedes(c.key[j], j, key, i)) return false;
                             if (collide64<D>(r, x, c.rad[j], img)) judge(j);
                             return any_acc;
@@ -553,7 +554,7 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
                             offq[d] = c.off[(uint64_t)i * D + d];
                         }
                         const float rf = __double2float_rn(r);
-                        visit_candidates_o(g, c, k, search_r2(r, g.rmax), [&](int32_t j, const int32_t* o, const int8_t* q) {
+                        visit_candidates_o(g, c, k, offq, search_r2(r, g.rmax), [&](int32_t j, const int32_t* o, const int8_t* q) {
                             if (!precedes(c.key[j], j, key, i)) return false;
                             if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) judge(j);
                             return any_acc;
@@ -762,13 +763,14 @@ __device__ __forceinline__ bool refine_mask64_body(const Grid<D>& g, const Geo<D
             centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cc[d], 0.5), p.len[d]));
         }
         int32_t k[D];
-        cell_of<D>(g, geo, centre, k);
+        float qo[D];  // the walk's query point: the voxel centre (every sphere that matters is within r_max + r_min of it)
+        cell_of_q<D>(g, geo, centre, k, qo);
         double pre0[K_PRE][D], pre1[K_PRE][D];
         uint64_t preR2[K_PRE];
         int npre = 0;
         bool overflow = false;
         const float R2q = search_r2(p.rmin, g.rmax);
-        const bool covered = visit_placed<D>(g, geo, k, R2q, [&](int64_t, const double* img, double rs) {
+        const bool covered = visit_placed<D>(g, geo, k, qo, R2q, [&](int64_t, const double* img, double rs) {
             visits++;
             const double R = __dadd_rn(rs, p.rmin);
             const uint64_t R2b = dbits(__dmul_rn(R, R));
@@ -823,7 +825,7 @@ __device__ __forceinline__ bool refine_mask64_body(const Grid<D>& g, const Geo<D
                 // the list was full: test every prefilter sphere again, straight from the grid
                 cov[0] = 0;
                 for (int w = 1; w < MASK_WORDS; w++) cov[w] = 0;
-                visit_placed<D>(g, geo, k, R2q, [&](int64_t, const double* img, double rs) {
+                visit_placed<D>(g, geo, k, qo, R2q, [&](int64_t, const double* img, double rs) {
                     const double R = __dadd_rn(rs, p.rmin);
                     const uint64_t R2b = dbits(__dmul_rn(R, R));
                     double dl0[D], dl1[D], s = 0.0;
@@ -945,7 +947,7 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
             return dbits(__dmul_rn(R, R));
         };
         const float R2q = search_r2(p.rmin, g.rmax);
-        const bool covered = visit_placed_o<D>(g, k, R2q, [&](int64_t idx, const int32_t* o, const int8_t* q) {
+        const bool covered = visit_placed_o<D>(g, k, relc, R2q, [&](int64_t idx, const int32_t* o, const int8_t* q) {
             visits++;
             const float rs = g.mono ? g.rmonof : g.radf[idx];
             const float R = __fadd_rn(rs, p.rminf);
@@ -1053,7 +1055,7 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
                 for (int w = 0; w < MASK_WORDS; w++) cov[w] = 0;
                 double orig[D], centre[D];
                 exact_corners(orig, centre);
-                visit_placed<D>(g, geo, k, R2q, [&](int64_t idx, const double* img, double rs) {
+                visit_placed<D>(g, geo, k, relc, R2q, [&](int64_t idx, const double* img, double rs) {
                     const double R = __dadd_rn(rs, p.rmin);
                     const uint64_t R2b = dbits(__dmul_rn(R, R));
                     double dl0[D], dl1[D], ss = 0.0;
@@ -1172,7 +1174,7 @@ __global__ void k_check(Grid<D> g, Geo<D> geo, unsigned long long* overlaps, uns
         rem /= g.n[d];
     }
     unsigned long long cnt = 0;
-    visit_placed<D>(g, geo, kc, search_r2(r, g.rmax), [&](int64_t j, const double* img, double rs) {
+    visit_placed<D>(g, geo, kc, nullptr, search_r2(r, g.rmax), [&](int64_t j, const double* img, double rs) {
         if (j > idx && collide64<D>(r, x, rs, img)) cnt++;
         return false;
     });

@@ -106,6 +106,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(const uint32_t* cou
     }
 }
 
+// 16-bit digit histogram of v = key >> S over the keys whose digits above it equal prefix (radix select):
+// the digit is (v >> dshift) & 0xFFFF, the prefix (v >> pshift), pshift = 64 for the top digit (no prefix).
+__global__ void k_key_digit_hist(const uint64_t* keys, uint64_t n, int S, int dshift, int pshift, uint64_t prefix,
+                                 uint32_t* hist) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = keys[i] >> S;
+        if (pshift >= 64 || (v >> pshift) == prefix) atomicAdd(hist + ((v >> dshift) & 0xFFFFu), 1u);
+    }
+}
+
 __global__ void __launch_bounds__(OCC_BLOCK) k_occ_block_counts(const uint32_t* occ, int64_t nwords, uint32_t* counts) {
     const int64_t w = (int64_t)blockIdx.x * OCC_BLOCK + threadIdx.x;
     const uint32_t c = w < nwords ? (uint32_t)__popc(occ[w]) : 0u;
@@ -125,6 +135,15 @@ void launch_scan_blocks(const uint32_t* counts, uint64_t* offsets, uint64_t n, u
     k_scan_tile_bases<<<1, SCAN_THREADS, 0, s>>>(offsets, n, tiles);
     if (tiles) k_scan_tiles<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(counts, offsets, n);
     count_launch(tiles ? 3 : 1);
+}
+
+void launch_key_digit_hist(const uint64_t* keys, uint64_t n, int S, int dshift, int pshift, uint64_t prefix,
+                           uint32_t* hist, cudaStream_t s) {
+    cudaMemsetAsync(hist, 0, 65536 * sizeof(uint32_t), s);
+    if (n == 0) return;
+    const uint64_t nb = (n + 255) / 256;
+    k_key_digit_hist<<<(unsigned)(nb < 152 * 16 ? nb : 152 * 16), 256, 0, s>>>(keys, n, S, dshift, pshift, prefix, hist);
+    count_launch();
 }
 
 void launch_occ_block_counts(const uint32_t* occ, int64_t nwords, uint32_t* counts, cudaStream_t s) {

@@ -55,6 +55,7 @@ struct Grid {
     int R;
     const float* rows_r2;  // per row: squared distance to its nearest cell along dimensions 1..D-1 (rows sorted by it)
     float c0f;             // cell edge along dimension 0
+    float inv_c0f;         // its inverse
     double rmax;           // largest radius the grid holds
     // FP32 screening representation of the placed centres (guard-band form): off = centre minus the
     // corner of its cell, rounded to float; radf = radius rounded to float
@@ -183,25 +184,56 @@ __device__ __forceinline__ uint32_t occ_bits(const uint32_t* occ, int64_t lin, i
     return len >= 32 ? bits : (bits & ((1u << len) - 1u));
 }
 
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Walks the stencil row by row: for each row, the wrapped cell coordinates of dimensions 1..D-1 and up to
 // three contiguous segments along dimension 0 (left wrap, inside, right wrap).  g(base, lo, hi, q, row) is
-// called per segment [lo, hi] with the image shifts q; it returns true to stop.
+// called per segment [lo, hi] with the image shifts q; it returns true to stop.  With query offsets qo, only
+// cells whose nearest point lies within sqrt(R2q) of the query point are walked: the query is cell k at offset
+// qo from its corner (FP32), each row is cut by the point's distance to it along dimensions 1..D-1, and its
+// dimension-0 range by the remaining distance.  R2q carries a 1e-4 margin, far above the float error of these
+// bounds.  Without (qo null) the rows are cut by the distance from the query's whole cell: the lanes of a warp
+// then walk the same cells in step, which the FP64 candidate kernels need (on this GPU a divergent FP64
+// instruction costs 16 SM cycles whatever the number of lanes it serves).
 template <int D, class G>
-__device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, int R, const float* rows_r2, float c0f,
-                                          float R2q, const int32_t* k, G&& g) {
+__device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, int R, const float* rows_r2,
+                                          const float* cf, float inv_c0, float R2q, const int32_t* k, const float* qo,
+                                          G&& g) {
     for (int r = 0; r < R; r++) {
-        // only cells that may hold a point within sqrt(R2q) of the query cell: rows by nearest distance, and
-        // along dimension 0 the offsets |o_0| <= 1 + sqrt(R2q - row distance) / c0
-        const float rest = rows_r2[r];
-        if (rest > R2q) break;
+        // rows in order of their nearest cell-to-cell distance: none after the first one beyond R2q
+        if (rows_r2[r] > R2q) break;
         const int8_t* row = rows + r * (D + 1);
-        // o0max = 1 + floor(sqrt(R2q - rest) / c0) without a square root or a division: the largest j with
-        // j^2 c0^2 <= R2q - rest, counted up to the row's own extent (R2q carries a 1e-4 margin, far above the
-        // float rounding of either form)
-        const float avail = R2q - rest, c0sq = c0f * c0f;
-        const int32_t ext = 1 + max(-(int32_t)row[0], (int32_t)row[1]);
-        int32_t o0max = 1;
-        while (o0max < ext && __fmul_rn((float)(o0max * o0max), c0sq) <= avail) o0max++;
+        int32_t olo, ohi;
+        if (qo) {
+            float rest = 0.f;
+#pragma unroll
+            for (int d = 1; d < D; d++) {
+                const int32_t o = row[1 + d];
+                const float gap = o > 0 ? __fsub_rn(__fmul_rn((float)o, cf[d]), qo[d])
+                                        : (o < 0 ? __fsub_rn(qo[d], __fmul_rn((float)(o + 1), cf[d])) : 0.f);
+                rest = __fadd_rn(rest, __fmul_rn(gap, gap));
+            }
+            if (rest > R2q) continue;
+            // dimension 0: offset o > 0 is within reach iff o c0 - q0 <= s, o < 0 iff q0 - (o + 1) c0 <= s
+            const float sr = sqrt_approx(__fsub_rn(R2q, rest));
+            const int32_t up = __float2int_rd(__fmul_rn(__fadd_rn(sr, qo[0]), inv_c0));
+            const int32_t dn = -1 - __float2int_rd(__fmul_rn(__fsub_rn(sr, qo[0]), inv_c0));
+            olo = max((int32_t)row[0], min(dn, 0));
+            ohi = min((int32_t)row[1], max(up, 0));
+        } else {
+            // cell-based range: |o_0| <= 1 + sqrt(R2q - row distance) / c0, as the largest j with
+            // j^2 c0^2 <= R2q - rest (no square root, no division), up to the row's own extent
+            const float avail = R2q - rows_r2[r], c0sq = cf[0] * cf[0];
+            const int32_t ext = 1 + max(-(int32_t)row[0], (int32_t)row[1]);
+            int32_t o0max = 1;
+            while (o0max < ext && __fmul_rn((float)(o0max * o0max), c0sq) <= avail) o0max++;
+            olo = max((int32_t)row[0], -o0max);
+            ohi = min((int32_t)row[1], o0max);
+        }
         int8_t q[D];
         int64_t base = 0;
 #pragma unroll
@@ -214,7 +246,7 @@ __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, 
             base = base * n[d] + kk;
         }
         base *= n[0];
-        const int32_t a = k[0] + max((int32_t)row[0], -o0max), b = k[0] + min((int32_t)row[1], o0max);
+        const int32_t a = k[0] + olo, b = k[0] + ohi;
         if (a < 0) {
             q[0] = -1;
             if (g(base, a + n[0], (b < 0 ? b : -1) + n[0], q, row)) return true;
@@ -232,10 +264,26 @@ __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, 
     return false;
 }
 
+// cell_of and the walk's query offsets together: the offset is the fraction of the cell coordinate that
+// cell_of already forms, times the cell edge (two more FP64-pipe instructions per dimension)
+template <int D>
+__device__ __forceinline__ void cell_of_q(const Grid<D>& g, const Geo<D>& geo, const double* x, int32_t* k, float* qo) {
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const double y = __dmul_rn(__dsub_rn(x[d], geo.inf[d]), g.inv_c[d]);
+        const double fl = floor(y);
+        int32_t kk = (int32_t)fl;
+        kk = kk < 0 ? 0 : (kk >= g.n[d] ? g.n[d] - 1 : kk);
+        k[d] = kk;
+        qo[d] = __fmul_rn(__double2float_rn(__dsub_rn(y, (double)kk)), g.cf[d]);
+    }
+}
+
 // Visits the placed spheres in the stencil around cell k; f(idx, img, r) returns true to stop.
 template <int D, class F>
-__device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo, const int32_t* k, float R2q, F&& f) {
-    return walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.c0f, R2q, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
+__device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo, const int32_t* k, const float* qo,
+                                             float R2q, F&& f) {
+    return walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.cf, g.inv_c0f, R2q, k, qo, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t*) {
         for (int32_t x = lo; x <= hi; x += 32) {
             const int len = hi - x + 1 < 32 ? hi - x + 1 : 32;
             uint32_t bits = occ_bits(g.occ, base + x, len);
@@ -257,8 +305,8 @@ __device__ __forceinline__ bool visit_placed(const Grid<D>& g, const Geo<D>& geo
 // Visits the placed spheres in the stencil around cell k with their integer cell offset o (the periodic
 // shift folded in: o = cell of the image - k); f(idx, o, q) returns true to stop.
 template <int D, class F>
-__device__ __forceinline__ bool visit_placed_o(const Grid<D>& g, const int32_t* k, float R2q, F&& f) {
-    return walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.c0f, R2q, k, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
+__device__ __forceinline__ bool visit_placed_o(const Grid<D>& g, const int32_t* k, const float* qo, float R2q, F&& f) {
+    return walk_rows<D>(g.n, g.rows, g.R, g.rows_r2, g.cf, g.inv_c0f, R2q, k, qo, [&](int64_t base, int32_t lo, int32_t hi, const int8_t* q, const int8_t* row) {
         int32_t o[D];
 #pragma unroll
         for (int d = 1; d < D; d++) o[d] = row[1 + d];

@@ -203,6 +203,10 @@ const DimOps* dim_ops(int D);
 // dimension-independent kernels (kernels_common.cu)
 void launch_scan_blocks(const uint32_t* counts, uint64_t* offsets, uint64_t n, uint64_t* total, cudaStream_t s);
 void launch_occ_block_counts(const uint32_t* occ, int64_t nwords, uint32_t* counts, cudaStream_t s);
+// 65536-bin histogram (zeroed first) of the 16-bit digit (key >> S >> dshift) & 0xFFFF over the keys with
+// (key >> S) >> pshift == prefix (pshift = 64: all keys)
+void launch_key_digit_hist(const uint64_t* keys, uint64_t n, int S, int dshift, int pshift, uint64_t prefix,
+                           uint32_t* hist, cudaStream_t s);
 uint64_t kernel_launch_count();
 void count_launch(int n = 1);
 // text returned by rsagpu_last_error() for the calling thread

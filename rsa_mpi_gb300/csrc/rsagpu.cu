@@ -6,6 +6,7 @@
 // Allreduce counters become device counters read once per round.
 #include <algorithm>
 #include <chrono>
+#include <map>
 #include <cmath>
 #include <random>
 #include <cstdarg>
@@ -145,6 +146,7 @@ struct rsagpu_algo {
     uint64_t blocks_cap = 0;
     uint32_t* d_err = nullptr;
     unsigned long long* d_visits = nullptr;
+    uint32_t* d_sel_hist = nullptr;  // digit histogram of the count cap's radix selection
     uint64_t placed = 0;              // spheres in the grid
     std::vector<double> mask_ms, mask_bytes, mask_voxels;  // per refine_mask launch
     // candidates
@@ -186,6 +188,7 @@ struct rsagpu_algo {
         dfree(block_offsets);
         dfree(d_err);
         dfree(d_visits);
+        dfree(d_sel_hist);
         dfree(d_mlp);
         dfree(d_feat);
         if (h_counters) cudaFreeHost(h_counters);
@@ -564,43 +567,88 @@ void refine(rsagpu_algo* A) {
     A->stats.peak_voxels = std::max(A->stats.peak_voxels, total);
 }
 
-// median_of_medians::find_pivot_for_first_elements with one rank (median_of_medians.ixx:8-157):
-// the pivot retain_only_first_elements compares priorities with.  Returns false where the reference
-// throws.
-uint64_t pivot_count(const std::vector<uint64_t>& v, double pivot) {
-    const uint64_t pv = (uint64_t)pivot;
-    return (uint64_t)(std::upper_bound(v.begin(), v.end(), pv) - v.begin());
-}
+// Order statistics and rank counts of v = key >> S over keys on the device, by radix selection with 16-bit
+// digit histograms (each a pass over the keys and a 256 KB copy, cached per digit prefix).
+struct DeviceSelect {
+    const uint64_t* keys;
+    uint64_t n;
+    int S, L;  // value shift, 16-bit digits per value
+    uint32_t* d_hist;
+    cudaStream_t st;
+    std::map<std::pair<int, uint64_t>, std::vector<uint64_t>> cum;  // (level, prefix) -> inclusive prefix sums
+    const std::vector<uint64_t>& hist(int level, uint64_t prefix) {
+        auto it = cum.find({level, prefix});
+        if (it != cum.end()) return it->second;
+        const int dshift = 16 * (L - 1 - level);
+        const int pshift = level == 0 ? 64 : 16 * (L - level);
+        launch_key_digit_hist(keys, n, S, dshift, pshift, prefix, d_hist, st);
+        std::vector<uint32_t> h(65536);
+        CK(cudaMemcpyAsync(h.data(), d_hist, 65536 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        std::vector<uint64_t> c(65536);
+        uint64_t run = 0;
+        for (int d = 0; d < 65536; d++) c[d] = (run += h[d]);
+        return cum.emplace(std::make_pair(level, prefix), std::move(c)).first->second;
+    }
+    // the rank-th smallest value (0-based)
+    uint64_t at(uint64_t rank) {
+        uint64_t prefix = 0;
+        for (int level = 0; level < L; level++) {
+            const std::vector<uint64_t>& c = hist(level, prefix);
+            const int d = (int)(std::upper_bound(c.begin(), c.end(), rank) - c.begin());
+            if (d > 0) rank -= c[d - 1];
+            prefix = (prefix << 16) | (uint64_t)d;
+        }
+        return prefix;
+    }
+    // the number of values <= t
+    uint64_t count_le(uint64_t t) {
+        if (L < 4 && (t >> (16 * L)) != 0) return n;
+        uint64_t total = 0, prefix = 0;
+        for (int level = 0; level < L; level++) {
+            const int d = (int)((t >> (16 * (L - 1 - level))) & 0xFFFFu);
+            const std::vector<uint64_t>& c = hist(level, prefix);
+            if (d > 0) total += c[d - 1];
+            if (level == L - 1) total += c[d] - (d > 0 ? c[d - 1] : 0);
+            prefix = (prefix << 16) | (uint64_t)d;
+        }
+        return total;
+    }
+};
 
-bool reference_pivot(std::vector<uint64_t> v, int64_t n_first, double* out) {
-    const int64_t n = (int64_t)v.size();
+// median_of_medians::find_pivot_for_first_elements with one rank (median_of_medians.ixx:8-157): the pivot
+// retain_only_first_elements compares priorities with, from the priorities' order statistics (at) and rank
+// counts (count_le of the integer part of a pivot; upper_bound over the sorted priorities in the reference).
+// Returns false where the reference throws.
+template <class At, class CountLe>
+bool reference_pivot(int64_t n, int64_t n_first, At&& at, CountLe&& count_le, double* out) {
     if (n_first > n || n_first <= 0 || n == 0) return false;
+    auto pivot_count = [&](double pivot) { return count_le((uint64_t)pivot); };
     const double pct = n_first / (1. * n);
-    std::sort(v.begin(), v.end());
     int64_t piv = (int64_t)(n * pct) - 1;
     int64_t mn = piv, mx = piv + 1;
     if (std::fabs(n * pct - 1 - piv) < 1e-8) mn -= 1;
     if (mn < 0) mn = 0;
     if (std::fabs(n * pct - 1 - piv - 1) < 1e-8) mx += 1;
     if (mx > n - 1) mx = n - 1;
-    double cand[2] = {(double)v[mn] - 2.220446049250313e-16, (double)v[mx] + 2.220446049250313e-16};
+    double cand[2] = {(double)at(mn) - 2.220446049250313e-16, (double)at(mx) + 2.220446049250313e-16};
     if ((uint64_t)cand[1] < (uint64_t)cand[0]) std::swap(cand[0], cand[1]);
     int p = 2;
     for (int i = 0; i < 2; i++)
-        if ((uint64_t)n_first <= pivot_count(v, cand[i])) {
+        if ((uint64_t)n_first <= pivot_count(cand[i])) {
             p = i;
             break;
         }
     if (p == 2) return false;
     double pmax = cand[p], pivot = pmax;
-    uint64_t below = pivot_count(v, pivot);
+    uint64_t below = pivot_count(pivot);
     if (below != (uint64_t)n_first) {
         if (p == 0) return false;
         const double pmin = cand[p - 1];
         double add = 0.5 * (pmax - pmin);
         for (int j = 0; j < 20; j++) {
             pivot = pmin + add;
-            below = pivot_count(v, pivot);
+            below = pivot_count(pivot);
             if (below == (uint64_t)n_first) break;
             if (below > (uint64_t)n_first) add = 0.5 * std::fabs(add);
             if (below < (uint64_t)n_first) add = -0.5 * std::fabs(add);
@@ -675,23 +723,20 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
         const uint64_t nacc = A->h_counters[3];
         greedy = nacc;
         if (nacc > max_new) {
-            std::vector<uint64_t> keys(nacc);
-            CK(cudaMemcpyAsync(keys.data(), c.gather, nacc * sizeof(uint64_t), cudaMemcpyDeviceToHost, A->stream));
-            CK(cudaStreamSynchronize(A->stream));
+            // the cap's order statistics by radix selection on the device (no copy or sort of the keys)
+            if (!A->d_sel_hist) A->d_sel_hist = dalloc<uint32_t>(65536);
             if (A->cap_rule == RSAGPU_CAP_EXACT) {
-                uint64_t cut = 0;
                 if (max_new > 0) {
-                    std::nth_element(keys.begin(), keys.begin() + (max_new - 1), keys.end());
-                    cut = keys[max_new - 1];
-                    ops->cut_accepted(c, 0, 0.0, cut, A->stream);
+                    DeviceSelect sel{c.gather, nacc, 0, 4, A->d_sel_hist, A->stream, {}};
+                    ops->cut_accepted(c, 0, 0.0, sel.at(max_new - 1), A->stream);
                 } else {
                     ops->cut_accepted(c, 1, -1.0, 0, A->stream);
                 }
             } else {
-                std::vector<uint64_t> pri(nacc);
-                for (uint64_t i = 0; i < nacc; i++) pri[i] = keys[i] >> 32;
+                DeviceSelect sel{c.gather, nacc, 32, 2, A->d_sel_hist, A->stream, {}};
                 double pivot = 0;
-                if (!reference_pivot(pri, (int64_t)max_new, &pivot))
+                if (!reference_pivot((int64_t)nacc, (int64_t)max_new, [&](int64_t r) { return sel.at((uint64_t)r); },
+                                     [&](uint64_t t) { return sel.count_le(t); }, &pivot))
                     raise(RSAGPU_ERR_PIVOT, "count-cap pivot search failed (%llu accepted, cap %llu)",
                           (unsigned long long)nacc, (unsigned long long)max_new);
                 ops->cut_accepted(c, 1, pivot, 0, A->stream);
