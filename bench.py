@@ -108,6 +108,17 @@ FORM_NAMES = {0: "plain FP64", 1: "FP32 screen + FP64 guard-band retest"}
 FORM_KERNEL = {0: "k_refine_mask", 1: "k_refine_mask32"}
 
 
+def aggregate(times, counts, dist=None, device="cpu"):
+    """Whole-job figures of N replicas: the max over ranks of each time, the sum of each count."""
+    import torch
+    t = torch.tensor(times, dtype=torch.float64, device=device)
+    c = torch.tensor(counts, dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return t.tolist(), c.tolist()
+
+
 def run_gpu_step(dim, L, r, seed, form=1):
     from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator
     rg = RadiusGenerator(dim, [(r, 1.0, 0)], volume=float(math.prod(L)))
@@ -392,13 +403,8 @@ def main():
         e2e_n += k
         e2e_s += s
         d2h = b
-    t = torch.tensor([dev_ms, wall, e2e_s], dtype=torch.float64, device="cuda")
-    tot = torch.tensor([float(spheres), float(e2e_n)], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
-    dev_ms_max, wall_max, e2e_max = t.tolist()
-    spheres_all, e2e_all = tot.tolist()
+    (dev_ms_max, wall_max, e2e_max), (spheres_all, e2e_all) = aggregate(
+        [dev_ms, wall, e2e_s], [float(spheres), float(e2e_n)], dist, "cuda")
     if rank != 0:
         if dist:
             dist.destroy_process_group()
