@@ -145,8 +145,8 @@ __global__ void __launch_bounds__(512, 2) k_b_probe(BatchArgs b, CandArgs c) {
     if (i < c.n && c.state[i] == ST_UNDECIDED) {
         const uint32_t s = b.cinst[i];
         const BInst& I = ((const BInst*)b.table)[s];
-        const Grid<D> g = I.g;
-        const Geo<D> geo = I.geo;
+        const Grid<D>& g = I.g;
+        const Geo<D>& geo = I.geo;
         alive = probe_body<F32>(g, geo, with_instance(c, b, I, s), i, rt);
     }
     const uint32_t slot = warp_append(&c.counters[0], alive);
@@ -167,8 +167,8 @@ __global__ void __launch_bounds__(512, 2) k_b_collect(BatchArgs b, CandArgs c) {
     if (t < nalive) {
         const uint32_t i = c.alive[t];
         const BInst& I = ((const BInst*)b.table)[b.cinst[i]];
-        const Grid<D> g = I.g;
-        const Geo<D> geo = I.geo;
+        const Grid<D>& g = I.g;
+        const Geo<D>& geo = I.geo;
         undecided = collect_body<F32>(g, geo, with_lists(c, I), i, rt);
     }
     const uint32_t mask = __ballot_sync(0xffffffffu, undecided);
@@ -194,8 +194,8 @@ __global__ void __launch_bounds__(512, 2) k_b_settle(BatchArgs b, CandArgs c, in
         if (t < nalive) {
             const uint32_t i = c.alive[t];
             const BInst& I = ((const BInst*)b.table)[b.cinst[i]];
-            const Grid<D> g = I.g;
-            const Geo<D> geo = I.geo;
+            const Grid<D>& g = I.g;
+            const Geo<D>& geo = I.geo;
             still = settle_body<F32>(g, geo, with_lists(c, I), i, rt);
         }
         const uint32_t mask = __ballot_sync(0xffffffffu, still);
@@ -218,8 +218,8 @@ __global__ void __launch_bounds__(256) k_b_commit(BatchArgs b, CandArgs c) {
         const uint32_t i = c.alive[t];
         s = b.cinst[i];
         const BInst& I = ((const BInst*)b.table)[s];
-        const Grid<D> g = I.g;
-        const Geo<D> geo = I.geo;
+        const Grid<D>& g = I.g;
+        const Geo<D>& geo = I.geo;
         acc = commit_body(g, geo, with_lists(c, I), i);
     }
     const uint32_t mask = __ballot_sync(0xffffffffu, acc);
@@ -245,8 +245,8 @@ __global__ void __launch_bounds__(512, 2) k_b_refine_mask(BatchArgs b, RefineArg
             mask[0] = 1u;
         } else {
             const BInst& I = ((const BInst*)b.table)[s];
-            const Grid<D> g = I.g;
-            const Geo<D> geo = I.geo;
+            const Grid<D>& g = I.g;
+            const Geo<D>& geo = I.geo;
             RefineParams p;
             p.V = 0;
             p.vin = nullptr;

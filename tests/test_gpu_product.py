@@ -56,6 +56,33 @@ def test_fp32_guard_form_gives_the_fp64_form_output(dim, L, r):
     assert out[1][1]["maximal"] == 1
 
 
+@pytest.mark.parametrize("dim,L,classes", [
+    (4, [1.0, 1.0, 1.0, 1.0], [(0.08, 1.0, 0)]),
+    (5, [1.0] * 5, [(0.12, 1.0, 0)]),
+    (2, [1.0, 0.8], [(0.02, 0.3, 0), (0.01, 0.1, 1)]),
+    (3, [1.0, 1.0, 1.0], [(0.02, 0.2, 0), (0.01, 0.1, 1), (0.005, 0.02, 2)]),
+])
+def test_fp32_guard_form_matches_fp64_in_higher_dimensions_and_with_classes(dim, L, classes):
+    """The FP32 form's fixed-point maps, lazy dart positions and point-trimmed walks in D = 4, 5 and with
+    several radius classes (count caps included): the same spheres as the plain FP64 form, and no overlap."""
+    out = []
+    for form in (_lib.RSAGPU_FORM_FP64, _lib.RSAGPU_FORM_FP32_GUARD):
+        rg = RadiusGenerator(dim, classes, volume=float(np.prod(L)))
+        dom = Domain([0.0] * dim, L, rg.max_radius)
+        algo = Algo(dom, rg, 6000)
+        algo.set_form(form)
+        algo.proceed(5)
+        pos, rad, ph = dom.arrays()
+        out.append((pos, rad, ph, algo.stats()))
+        assert dom.check() == (0, 0)
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
+    assert O.count_overlaps(dim, [0.0] * dim, L, out[1][0], out[1][1]) == 0
+    if len(classes) == 1:
+        assert out[1][3]["maximal"] == 1
+
+
 def test_product_runs_are_deterministic_per_seed():
     d1, _ = run_product(2, [1.0, 1.0], 0.01, 3)
     d2, _ = run_product(2, [1.0, 1.0], 0.01, 3)
