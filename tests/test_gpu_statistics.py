@@ -1,0 +1,76 @@
+"""The product path's output distribution against the reference's own algorithm (the oracle, which draws with
+the reference's std::mt19937 stream, ≈6000 darts per round and its miss-rate schedule).  The GPU draws with
+Philox, throws 10^4-10^7 darts per round and subdivides on another schedule; none of that may change the
+distribution of the maximal packing.  Compared over many seeds: the packing fraction and the pair-correlation
+function near contact, in both forms."""
+import functools
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from rsa_mpi_gb300 import _lib
+from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator
+
+pytestmark = pytest.mark.gpu
+
+R = 0.01
+SEEDS = 24
+EDGES = np.linspace(2.0, 3.0, 11)  # pair distances in units of r: contact to one diameter beyond
+
+
+def pair_histogram(pos, L=1.0):
+    """Pair counts per distance bin (periodic minimum image), distances in units of r."""
+    d = pos[:, None, :] - pos[None, :, :]
+    d -= L * np.round(d / L)
+    dist = np.sqrt((d * d).sum(-1))[np.triu_indices(len(pos), 1)] / R
+    return np.histogram(dist, EDGES)[0].astype(float)
+
+
+def normalised_g(pos):
+    # g(r) up to the common density factor: pair counts per shell area, per point
+    h = pair_histogram(pos)
+    shell = np.pi * (EDGES[1:] ** 2 - EDGES[:-1] ** 2)
+    return h / shell / len(pos)
+
+
+def gpu_samples(form):
+    out = []
+    for s in range(SEEDS):
+        rg = RadiusGenerator(2, [(R, 1.0, 0)], volume=1.0)
+        dom = Domain([0.0, 0.0], [1.0, 1.0], R)
+        algo = Algo(dom, rg, 6000)
+        algo.set_form(form)
+        algo.proceed(1000 + s)
+        assert algo.stats()["maximal"] == 1
+        out.append(dom.arrays()[0])
+        algo.close()
+        dom.close()
+    return out
+
+
+@functools.lru_cache(maxsize=1)
+def oracle_samples():
+    out = []
+    for s in range(SEEDS):
+        o = O.Oracle(2, [0.0, 0.0], [1.0, 1.0], [(R, 1.0, 0)])
+        o.proceed(2000 + s)
+        out.append(o.spheres()[0])
+    return tuple(out)
+
+
+def compare(a, b, what):
+    a, b = np.asarray(a), np.asarray(b)
+    ma, mb = a.mean(0), b.mean(0)
+    se = np.sqrt(a.var(0, ddof=1) / len(a) + b.var(0, ddof=1) / len(b))
+    z = np.abs(ma - mb) / np.maximum(se, 1e-12)
+    assert np.all(z < 4.5), (what, ma, mb, z)
+
+
+@pytest.mark.parametrize("form", [_lib.RSAGPU_FORM_FP32_GUARD, _lib.RSAGPU_FORM_FP64])
+def test_packing_distribution_matches_the_reference_algorithm(form):
+    gpu = gpu_samples(form)
+    ora = oracle_samples()
+    vol = np.pi * R * R
+    compare([len(p) * vol for p in gpu], [len(p) * vol for p in ora], "packing fraction")
+    compare([normalised_g(p) for p in gpu], [normalised_g(p) for p in ora], "g(r) near contact")
