@@ -111,6 +111,14 @@ public:
                                                      exclusion_distance, &g));
         ptr_ = std::shared_ptr<rsagpu_radgen>(g, [](rsagpu_radgen* q) { rsagpu_radgen_destroy(q); });
     }
+    // continuous radius law r_min + (r_max - r_min) x, x uniform in [0, 1): the internal
+    // sac_de_billes::RadiusGenerator<DIM>(min, max, &RandomRadiusGenerator(transform, phase), nb_spheres, 0)
+    // with the uniform transform (radius_generator.ixx:39-48)
+    static RadiusGenerator uniform(double r_min, double r_max, uint64_t nb_spheres, int phase) {
+        rsagpu_radgen* g = nullptr;
+        detail::check(rsagpu_radgen_create_uniform(DIM, r_min, r_max, nb_spheres, phase, &g));
+        return RadiusGenerator(std::shared_ptr<rsagpu_radgen>(g, [](rsagpu_radgen* q) { rsagpu_radgen_destroy(q); }));
+    }
     double get_max_radius() const {
         double v = 0;
         detail::check(rsagpu_radgen_max_radius(ptr_.get(), &v));
@@ -119,6 +127,7 @@ public:
     rsagpu_radgen* handle() const { return ptr_.get(); }
 
 private:
+    explicit RadiusGenerator(std::shared_ptr<rsagpu_radgen> p) : ptr_(std::move(p)) {}
     std::shared_ptr<rsagpu_radgen> ptr_;
 };
 

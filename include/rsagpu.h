@@ -79,6 +79,12 @@ int rsagpu_radgen_create_counts(int dim, const double* radii, const uint64_t* co
 int rsagpu_radgen_create_fractions(int dim, const double* radii, const double* fractions,
                                    const int* phases, int n_classes, double volume,
                                    double exclusion_distance, rsagpu_radgen** out);
+/* Continuous radius law: each dart's radius is r_min + (r_max - r_min) x, x uniform in [0, 1), and
+ * count spheres are wanted (10^16: run to maximality).  Replaces sac_de_billes::RadiusGenerator<DIM>(
+ * min_radius, max_radius, &RandomRadiusGenerator(transform, phase), nb_spheres, 0) with the uniform transform
+ * (radius_generator.ixx:39-48, radius_generator.hxx:12-38, test/test_random_radius_generator.cpp:13-29). */
+int rsagpu_radgen_create_uniform(int dim, double r_min, double r_max, uint64_t count, int phase,
+                                 rsagpu_radgen** out);
 int rsagpu_radgen_destroy(rsagpu_radgen* rg);
 int rsagpu_radgen_max_radius(const rsagpu_radgen* rg, double* out);
 int rsagpu_radgen_min_radius(const rsagpu_radgen* rg, double* out);

@@ -49,6 +49,8 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.ora_create.restype = C.c_void_p
         L.ora_create.argtypes = [C.c_int, _d, _d, C.c_double, C.c_int, _d, _u64, _i32, C.c_double, C.c_int]
+        L.ora_create_uniform.restype = C.c_void_p
+        L.ora_create_uniform.argtypes = [C.c_int, _d, _d, C.c_double, C.c_double, C.c_uint64, C.c_int, C.c_int]
         L.ora_destroy.argtypes = [C.c_void_p]
         L.ora_count_from_fraction.restype = C.c_uint64
         L.ora_count_from_fraction.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double]
@@ -135,6 +137,20 @@ class Oracle:
                                _p(r, _d), _p(n, _u64), _p(ph, _i32), exclusion, nbshots)
         if not self._h:
             raise RuntimeError("oracle: invalid configuration")
+
+    @classmethod
+    def uniform(cls, dim, inf, sup, r_min, r_max, count=10**16, phase=0, nbshots=6000):
+        """A continuous radius law: each dart's radius r_min + (r_max - r_min) x, x ~ U[0, 1)
+        (RadiusGenerator with a RandomRadiusGenerator, radius_generator.ixx:39-48)."""
+        self = cls.__new__(cls)
+        self.dim = dim
+        self.inf = np.ascontiguousarray(inf, dtype=np.float64)
+        self.sup = np.ascontiguousarray(sup, dtype=np.float64)
+        self._h = lib().ora_create_uniform(dim, _p(self.inf, _d), _p(self.sup, _d), float(r_min), float(r_max),
+                                           int(count), int(phase), int(nbshots))
+        if not self._h:
+            raise RuntimeError("oracle: invalid configuration")
+        return self
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -18,6 +18,12 @@
  * voxels) on stdout.  The final spheres are written to <out.bin>:
  *   int32 dim, int64 n, then n records of {double center[dim], double radius, int32 phase}.
  * The wall time of proceed() alone is printed as "proceed_seconds <t>".
+ *
+ *   ref_rsa runu <dim> <seed> <nbshots> <L_0..L_{D-1}> <r_min> <r_max> <count> <phase> <out.bin>
+ *
+ * The same run with a continuous radius law: sac_de_billes::RandomRadiusGenerator with the transform
+ * x -> r_min + (r_max - r_min) x of a uniform x (radius_generator.hxx:12-38, the uniform law of
+ * test/test_random_radius_generator.cpp:13-29), <count> spheres wanted.
  */
 #include <chrono>
 #include <cstdio>
@@ -85,9 +91,72 @@ int run(int argc, char** argv) {
     return 0;
 }
 
+template<int DIM>
+int write_spheres(rsa_domain<DIM>& domain, const std::string& out) {
+    auto spheres = domain.extract_spheres();
+    FILE* f = std::fopen(out.c_str(), "wb");
+    if (!f) return 3;
+    int32_t dim = DIM;
+    int64_t n = spheres.size();
+    std::fwrite(&dim, sizeof(dim), 1, f);
+    std::fwrite(&n, sizeof(n), 1, f);
+    for (const auto& s : spheres) {
+        std::fwrite(s.center.data(), sizeof(double), DIM, f);
+        double r = s.radius;
+        int32_t ph = s.phase;
+        std::fwrite(&r, sizeof(r), 1, f);
+        std::fwrite(&ph, sizeof(ph), 1, f);
+    }
+    std::fclose(f);
+    std::printf("spheres %lld volume_of_spheres %.17g\n", (long long)n,
+        domain.compute_total_volume_of_spheres());
+    return 0;
+}
+
+template<int DIM>
+int run_uniform_radius(int argc, char** argv) {
+    // argv: runu dim seed nbshots L... r_min r_max count phase out
+    int a = 2;
+    size_t seed = std::strtoull(argv[a++], nullptr, 10);
+    int nbshots = std::atoi(argv[a++]);
+    std::array<double, DIM> inf{}, sup{};
+    for (int d = 0; d < DIM; d++) {
+        inf[d] = 0.;
+        sup[d] = std::strtod(argv[a++], nullptr);
+    }
+    const double r_min = std::strtod(argv[a++], nullptr);
+    const double r_max = std::strtod(argv[a++], nullptr);
+    const uint64_t count = std::strtoull(argv[a++], nullptr, 10);
+    const uint64_t phase = std::strtoull(argv[a++], nullptr, 10);
+    std::string out = argv[a++];
+    if (a > argc) return 2;
+    auto transform = [r_min, r_max](double x) { return r_min + (r_max - r_min) * x; };
+    sac_de_billes::RandomRadiusGenerator random_radius(transform, phase);
+    sac_de_billes::RadiusGenerator<DIM> radius_generator(r_min, r_max, &random_radius, count, 0.);
+    rsa_domain<DIM> domain(inf, sup, 1, radius_generator.get_max_radius());
+    auto t0 = std::chrono::steady_clock::now();
+    algorithm::uniform_generate<DIM, 1, true>(domain, radius_generator, nbshots, 10, seed);
+    auto t1 = std::chrono::steady_clock::now();
+    std::printf("proceed_seconds %.6f\n", std::chrono::duration<double>(t1 - t0).count());
+    return write_spheres<DIM>(domain, out);
+}
+
 } // namespace
 
 int main(int argc, char** argv) {
+    if (argc >= 3 && std::string(argv[1]) == "runu") {
+        int dim = std::atoi(argv[2]);
+        argv[2] = argv[1];
+        argv++;
+        argc--;
+        switch (dim) {
+        case 2: return run_uniform_radius<2>(argc, argv);
+        case 3: return run_uniform_radius<3>(argc, argv);
+        default:
+            std::fprintf(stderr, "dim %d not built\n", dim);
+            return 2;
+        }
+    }
     if (argc < 3 || std::string(argv[1]) != "run") {
         std::fprintf(stderr, "usage: ref_rsa run <dim> <seed> <nbshots> <volume_mode> <L...> <k> (<r> <phi> <phase>)* <out>\n");
         return 2;

@@ -449,6 +449,9 @@ struct rsa_oracle {
     uint8_t* tr_ref;
     uint64_t last_round_vox;
     int cap_exact;
+    /* continuous radius law: radius = r_min + (r_max - r_min) x, x ~ U[0, 1) */
+    int uniform_radius;
+    int uniform_phase;
 };
 
 rsa_oracle* ora_create(int dim, const double* inf, const double* sup, double domain_rad,
@@ -489,6 +492,25 @@ rsa_oracle* ora_create(int dim, const double* inf, const double* sup, double dom
     o->cls_idx = 0;
     double search = 2 * (o->r_max > domain_rad ? o->r_max : domain_rad);
     store_init(&o->st, dim, o->inf, o->L, search);
+    return o;
+}
+
+/* RadiusGenerator(min_radius, max_radius, &RandomRadiusGenerator(transform, phase), nb_spheres, 0)
+ * (radius_generator.ixx:39-48, radius_generator.hxx:12-38) with transform x -> r_min + (r_max - r_min) x:
+ * one entry (radius 0, nb_spheres, phase 0) in the class list, explicit r_min and r_max, every dart's
+ * radius drawn after the priorities (generate_candidates, operator_algorithm.ixx:568-582). */
+rsa_oracle* ora_create_uniform(int dim, const double* inf, const double* sup, double r_min, double r_max,
+    uint64_t count, int phase, int nbshots) {
+    const double r0 = 0.;
+    const int ph0 = 0;
+    rsa_oracle* o = ora_create(dim, inf, sup, r_max, 1, &r0, &count, &ph0, 0., nbshots);
+    if (!o) return NULL;
+    o->r_min = r_min;
+    o->r_max = r_max;
+    o->uniform_radius = 1;
+    o->uniform_phase = phase;
+    store_free(&o->st);
+    store_init(&o->st, dim, o->inf, o->L, 2 * r_max);
     return o;
 }
 
@@ -1045,9 +1067,17 @@ int ora_gen_round(rsa_oracle* o, uint64_t* n_out, uint64_t* max_new, int* may_ou
     }
     /* generate_priority<int> (operator_algorithm.ixx:373-381) */
     for (uint64_t i = 0; i < n; i++) o->ckey[i] = ora_uniform_int(&o->g, 0u, (uint32_t)INT_MAX);
-    for (uint64_t i = 0; i < n; i++) {
-        o->crad[i] = o->cls_r[o->cls_idx];
-        o->cphase[i] = o->cls_phase[o->cls_idx];
+    if (o->uniform_radius) {
+        /* RandomRadiusGenerator::operator() (radius_generator.hxx:27-34): law::uniform<double>(0, 1) */
+        for (uint64_t i = 0; i < n; i++) {
+            o->crad[i] = o->r_min + (o->r_max - o->r_min) * ora_canonical(&o->g);
+            o->cphase[i] = o->uniform_phase;
+        }
+    } else {
+        for (uint64_t i = 0; i < n; i++) {
+            o->crad[i] = o->cls_r[o->cls_idx];
+            o->cphase[i] = o->cls_phase[o->cls_idx];
+        }
     }
     o->ncand = n;
     *n_out = n;

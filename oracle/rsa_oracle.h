@@ -41,6 +41,11 @@ rsa_oracle* ora_create(int dim, const double* inf, const double* sup, double dom
     double exclusion_distance, int nbshots);
 void ora_destroy(rsa_oracle* o);
 
+/* A continuous radius law: radius = r_min + (r_max - r_min) x per dart, x ~ U[0, 1), <count> spheres wanted
+ * (RadiusGenerator with a RandomRadiusGenerator, radius_generator.ixx:39-48, radius_generator.hxx:12-38). */
+rsa_oracle* ora_create_uniform(int dim, const double* inf, const double* sup, double r_min, double r_max,
+    uint64_t count, int phase, int nbshots);
+
 /* uint64(volume * phi / v_D(r)) as compute_desired_radius_nb_phase (radius_generator.ixx:71-86). */
 uint64_t ora_count_from_fraction(int dim, double r, double phi, double volume);
 /* v_D(r) as sphereTools::volumeSphere (auxiliary/Geometry/Sphere.ixx:30-57). */

@@ -77,6 +77,7 @@ _SIGS = {
     "rsagpu_domain_extract": (C.c_int, [_vp, _d, _d, _i32, C.c_uint64, _u64]),
     "rsagpu_domain_check": (C.c_int, [_vp, _u64, _u64]),
     "rsagpu_radgen_create_counts": (C.c_int, [C.c_int, _d, _u64, _i32, C.c_int, C.c_double, C.POINTER(_vp)]),
+    "rsagpu_radgen_create_uniform": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint64, C.c_int, C.POINTER(_vp)]),
     "rsagpu_radgen_create_fractions": (C.c_int, [C.c_int, _d, _d, _i32, C.c_int, C.c_double, C.c_double,
                                                  C.POINTER(_vp)]),
     "rsagpu_radgen_destroy": (C.c_int, [_vp]),

@@ -112,6 +112,8 @@ struct DartParams {
     uint32_t seed_lo, seed_hi, round_lo, round_hi;
     double radius;
     int32_t phase;
+    int32_t rand_radius;  // continuous radius law: radius = r_lo + r_span x (dart_radius)
+    double r_lo, r_span;
     double* pos;
     uint64_t* key;
     double* rad;
@@ -136,6 +138,16 @@ struct DartParams {
     uint32_t* perm;
     uint32_t* err;         // error bits (ERR_DART_SLOT)
 };
+
+// radius of dart i: the class radius, or under a continuous law r_lo + r_span x with x the 53-bit uniform of
+// the dart's own Philox call in a separate counter space (call word 0x80000000), as the reference's transform
+// x -> r_min + (r_max - r_min) x (radius_generator.hxx:27-34)
+__device__ __forceinline__ double dart_radius(const DartParams& p, uint32_t i) {
+    if (!p.rand_radius) return p.radius;
+    const uint4 r = philox4x32_10(make_uint4(i, p.round_lo, p.round_hi, 0x80000000u), make_uint2(p.seed_lo, p.seed_hi));
+    const uint64_t bits = ((((uint64_t)r.x) << 32) | r.y) >> 11;
+    return __dadd_rn(p.r_lo, __dmul_rn(p.r_span, (double)bits * 0x1.0p-53));
+}
 
 // voxel drawn by dart i (the first Philox call's words 0 and 1)
 __device__ __forceinline__ uint64_t dart_voxel(const DartParams& p, uint32_t i) {
@@ -196,7 +208,7 @@ __device__ __forceinline__ void dart32_body(const DartParams& p, uint32_t i, uin
         p.off[o * D + d] = __fmul_rn(__fmul_rn(__uint2float_rn(fr), 0x1p-32f), p.cf[d]);
     }
     p.key[o] = ((uint64_t)w[2 + 2 * D] << 32) | i;
-    p.rad[o] = p.radius;
+    p.rad[o] = dart_radius(p, i);
     p.cphase[o] = p.phase;
     p.state[o] = ST_UNDECIDED;
 }
@@ -218,7 +230,7 @@ __device__ __forceinline__ void dart_body(const DartParams& p, uint32_t i, uint6
         p.pos[o * D + d] = __dadd_rn(orig, __dmul_rn(p.len[d], u));
     }
     p.key[o] = ((uint64_t)w[2 + 2 * D] << 32) | i;
-    p.rad[o] = p.radius;
+    p.rad[o] = dart_radius(p, i);
     p.cphase[o] = p.phase;
     p.state[o] = ST_UNDECIDED;
 }
@@ -1255,6 +1267,9 @@ void op_darts(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaStre
     p.round_hi = (uint32_t)(a.round >> 32);
     p.radius = a.radius;
     p.phase = a.phase;
+    p.rand_radius = a.rand_radius;
+    p.r_lo = a.r_lo;
+    p.r_span = a.r_span;
     p.pos = c.pos;
     p.key = c.key;
     p.rad = c.rad;
@@ -1307,6 +1322,9 @@ void op_darts32(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaSt
     p.round_hi = (uint32_t)(a.round >> 32);
     p.radius = a.radius;
     p.phase = a.phase;
+    p.rand_radius = a.rand_radius;
+    p.r_lo = a.r_lo;
+    p.r_span = a.r_span;
     p.pos = c.pos;
     p.key = c.key;
     p.rad = c.rad;

@@ -72,6 +72,8 @@ struct DartArgs {
     double radius;
     int32_t phase;
     uint64_t* vidx_out;  // optional: chosen voxel per dart
+    int32_t rand_radius;  // continuous radius law: radius = r_lo + r_span x, x from the dart's own Philox draw
+    double r_lo, r_span;
     uint64_t rho_frac[MAX_D];  // FP32-form darts: level-0 voxel length / cell edge (voxel_cell_ratio)
     uint32_t rho_int[MAX_D];
     int32_t level;             // voxel level (the fixed-point shift)

@@ -55,8 +55,13 @@ struct rsagpu_radgen {
     std::vector<int> phase;
     double excl = 0;
     int idx = 0;
-    double rmax() const { return r.front(); }
-    double rmin() const { return r.back(); }
+    // continuous radius law (RandomRadiusGenerator with x -> r_min + (r_max - r_min) x): one entry
+    // (radius 0, count, phase 0) in the class list, every dart's radius drawn (radius_generator.ixx:39-48)
+    bool uniform = false;
+    double u_rmin = 0, u_rmax = 0;
+    int u_phase = 0;
+    double rmax() const { return uniform ? u_rmax : r.front(); }
+    double rmin() const { return uniform ? u_rmin : r.back(); }
 };
 
 struct SphereGrid {
@@ -339,6 +344,17 @@ GridPlan plan_grid(int D, const double* inf, const double* L, double rmin, doubl
 namespace {
 
 void set_device(const rsagpu_domain* d) { CK(cudaSetDevice(d->device)); }
+
+// a continuous radius law draws each dart's radius: r_min + (r_max - r_min) x, the span rounded first as in
+// the transform of the reference's RandomRadiusGenerator
+void set_dart_radius_law(const rsagpu_radgen& rg, DartArgs* da) {
+    da->rand_radius = rg.uniform ? 1 : 0;
+    if (rg.uniform) {
+        da->r_lo = rg.u_rmin;
+        da->r_span = rg.u_rmax - rg.u_rmin;
+        da->phase = rg.u_phase;
+    }
+}
 
 // ------------------------------------------------------------------------------------------------
 // sphere grid: cells of edge c with c sqrt(D) < 2 r_min (at most one accepted centre per cell) and
@@ -905,6 +921,7 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         da.seed = seed;
         da.round = A->round++;
         da.radius = A->rg.r[A->rg.idx];
+        set_dart_radius_law(A->rg, &da);
         da.phase = A->rg.phase[A->rg.idx];
         const auto tp0 = std::chrono::steady_clock::now();
         ev_record(A, 0);
@@ -1192,6 +1209,25 @@ int rsagpu_radgen_create_fractions(int dim, const double* radii, const double* f
     });
 }
 
+int rsagpu_radgen_create_uniform(int dim, double r_min, double r_max, uint64_t count, int phase,
+                                 rsagpu_radgen** out) {
+    return guarded([&] {
+        if (!out) raise(RSAGPU_ERR_ARG, "null argument");
+        if (!(r_min > 0) || !(r_max >= r_min)) raise(RSAGPU_ERR_ARG, "need 0 < r_min <= r_max");
+        if (dim < 2 || dim > MAX_D) raise(RSAGPU_ERR_ARG, "dimension %d not supported (2..%d)", dim, MAX_D);
+        auto* rg = new rsagpu_radgen();
+        rg->dim = dim;
+        rg->r.push_back(0.0);
+        rg->n.push_back(count);
+        rg->phase.push_back(0);
+        rg->uniform = true;
+        rg->u_rmin = r_min;
+        rg->u_rmax = r_max;
+        rg->u_phase = phase;
+        *out = rg;
+    });
+}
+
 int rsagpu_radgen_destroy(rsagpu_radgen* rg) {
     delete rg;
     return RSAGPU_OK;
@@ -1233,7 +1269,7 @@ int rsagpu_algo_create(rsagpu_domain* dom, const rsagpu_radgen* rg, int nbshots,
             A->d_visits = dalloc<unsigned long long>(2);
             // the algo rebuilds the domain's grid and drops its spheres (operator_algorithm.ixx:25-26)
             build_grid(dom, rg->rmin(), std::max(rg->rmax(), 0.0));
-            dom->grid.a.mono = rg->r.size() == 1;
+            dom->grid.a.mono = rg->r.size() == 1 && !rg->uniform;
             dom->grid.a.rmono = rg->r.front();
             A->placed = 0;
             ensure_cand(A, 1024);
@@ -1356,7 +1392,7 @@ int rsagpu_algo_reset_radgen(rsagpu_algo* algo, const rsagpu_radgen* rg) {
         // spheres of the previous generator keep their radii: the grid's one-radius shortcut holds only if
         // the new generator has the same single radius
         GridArgs& ga = algo->dom->grid.a;
-        ga.mono = ga.mono && rg->r.size() == 1 && rg->r.front() == ga.rmono;
+        ga.mono = ga.mono && rg->r.size() == 1 && !rg->uniform && rg->r.front() == ga.rmono;
     });
 }
 
@@ -1481,6 +1517,7 @@ int rsagpu_algo_draw_darts(rsagpu_algo* algo, uint64_t seed, uint64_t round, uin
         da.seed = seed;
         da.round = round;
         da.radius = algo->rg.r[std::min<int>(algo->rg.idx, (int)algo->rg.r.size() - 1)];
+        set_dart_radius_law(algo->rg, &da);
         da.phase = 0;
         da.vidx_out = algo->cand.vidx;
         CandArgs c = cand_args(algo, (uint32_t)n);

@@ -96,6 +96,18 @@ class RadiusGenerator:
                                                        len(classes), float(volume), float(exclusion), C.byref(h)))
         self._h = h
 
+    @classmethod
+    def uniform(cls, dim: int, r_min: float, r_max: float, count: int = 10**16, phase: int = 0):
+        """Continuous radius law: each sphere's radius r_min + (r_max - r_min) x, x uniform in [0, 1)
+        (RadiusGenerator with a RandomRadiusGenerator, include/radius_generator.hxx:12-38); count spheres
+        wanted, 10^16 running to maximality."""
+        self = cls.__new__(cls)
+        self.dim = dim
+        h = C.c_void_p()
+        check(lib().rsagpu_radgen_create_uniform(dim, float(r_min), float(r_max), int(count), int(phase), C.byref(h)))
+        self._h = h
+        return self
+
     def __del__(self):
         if getattr(self, "_h", None):
             try:

@@ -26,5 +26,15 @@ int main() {
         return 3;
     } catch (const std::runtime_error&) {
     }
+    // continuous radius law (test/test_random_radius_generator.cpp:13-29: r uniform in [0.05, 0.055])
+    auto urg = user_interface::RadiusGenerator<DIM>::uniform(0.05, 0.055, 10000000000000000ull, 0);
+    user_interface::rsa_domain<DIM> ud({0., 0., 0.}, {1., 1., 1.}, urg.get_max_radius());
+    user_interface::rsa_algo<DIM> ualgo(ud, urg, 6000);
+    ualgo.proceed(0);
+    auto us = ud.extract_spheres();
+    std::printf("uniform radii: spheres %zu\n", us.size());
+    if (us.size() < 600 || us.size() > 760) return 4;
+    for (const auto& s : us)
+        if (s.radius < 0.05 || s.radius >= 0.055) return 5;
     return 0;
 }

@@ -51,6 +51,15 @@ CASES = {
     "n2d_rect_s7": (2, 7, 500, 0, [1.3, 0.7], [(0.02, 1.0, 0)]),
 }
 
+# continuous radius law (sac_de_billes::RandomRadiusGenerator, radius = r_min + (r_max - r_min) x):
+# name -> (dim, seed, nbshots, L, r_min, r_max, count, phase); count 10^16 runs to maximality
+UNIFORM_CASES = {
+    # the uniform law of the reference test test_random_radius_generator.cpp:13-29 (3D, r in [0.05, 0.055])
+    "u3d_r0.05-0.055_s0": (3, 0, 6000, [1.0, 1.0, 1.0], 0.05, 0.055, 10**16, 0),
+    "u2d_r0.02-0.025_s7": (2, 7, 6000, [1.0, 1.0], 0.02, 0.025, 10**16, 0),
+    "u2d_r0.01-0.0105_s3": (2, 3, 3000, [1.0, 1.0], 0.01, 0.0105, 10**16, 1),
+}
+
 
 def parse_trace(log: str):
     shots = [int(m.group(1)) for m in re.finditer(r"--> Miss rate = .*?Nb shots = (\d+) ; Nb miss", log)]
@@ -72,16 +81,25 @@ def main():
     ref = O.build_ref(args.reference)
     if ref is None:
         sys.exit("reference checkout not found")
-    index = {}
-    for name, (dim, seed, nbshots, vmode, L, classes) in CASES.items():
+    index_path = os.path.join(HERE, "index.json")
+    index = json.load(open(index_path)) if args.only and os.path.exists(index_path) else {}
+    jobs = [(name, spec, None) for name, spec in CASES.items()]
+    jobs += [(name, (dim, seed, nbshots, 0, L, []), (r0, r1, count, ph))
+             for name, (dim, seed, nbshots, L, r0, r1, count, ph) in UNIFORM_CASES.items()]
+    for name, (dim, seed, nbshots, vmode, L, classes), uniform in jobs:
         if args.only and args.only != name:
             continue
         out = os.path.join(ROOT, "_work", f"golden_{name}.bin")
         os.makedirs(os.path.dirname(out), exist_ok=True)
-        cmd = [ref, "run", str(dim), str(seed), str(nbshots), str(vmode)] + [repr(x) for x in L]
-        cmd += [str(len(classes))]
-        for r, phi, ph in classes:
-            cmd += [repr(r), repr(phi), str(ph)]
+        if uniform is None:
+            cmd = [ref, "run", str(dim), str(seed), str(nbshots), str(vmode)] + [repr(x) for x in L]
+            cmd += [str(len(classes))]
+            for r, phi, ph in classes:
+                cmd += [repr(r), repr(phi), str(ph)]
+        else:
+            r0, r1, count, ph = uniform
+            cmd = [ref, "runu", str(dim), str(seed), str(nbshots)] + [repr(x) for x in L]
+            cmd += [repr(r0), repr(r1), str(count), str(ph)]
         cmd += [out]
         env = dict(os.environ, OMP_NUM_THREADS="8")
         log = subprocess.run(cmd, check=True, capture_output=True, text=True, env=env).stdout
@@ -95,10 +113,11 @@ def main():
         index[name] = dict(dim=dim, seed=seed, nbshots=nbshots, volume_mode=vmode, L=L,
                            classes=[list(x) for x in classes], n_spheres=int(len(r)),
                            volume_of_spheres=vol, rounds=int(len(shots)), ref_seconds_8threads=secs)
+        if uniform is not None:
+            index[name]["uniform"] = list(uniform)
         print(name, len(r), vol, len(shots), f"{secs:.3f}s")
-    if not args.only:
-        with open(os.path.join(HERE, "index.json"), "w") as f:
-            json.dump(index, f, indent=1)
+    with open(index_path, "w") as f:
+        json.dump(index, f, indent=1)
 
 
 if __name__ == "__main__":

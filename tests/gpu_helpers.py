@@ -26,6 +26,14 @@ def sort_voxels(v):
 def make_pair(case, cap_exact=False, form=0):
     """(oracle, gpu algo, gpu domain) for a golden case."""
     D = case["dim"]
+    if "uniform" in case:  # continuous radius law
+        r0, r1, count, ph = case["uniform"]
+        ora = O.Oracle.uniform(D, [0.0] * D, case["L"], r0, r1, count, ph, nbshots=case["nbshots"])
+        rg = RadiusGenerator.uniform(D, r0, r1, count, ph)
+        dom = Domain([0.0] * D, case["L"], rg.max_radius)
+        algo = Algo(dom, rg, case["nbshots"])
+        algo.set_form(form)
+        return ora, algo, dom
     vol = 1.0 if case["volume_mode"] == 1 else float(np.prod(case["L"]))
     classes = [tuple(x) for x in case["classes"]]
     ora = O.Oracle(D, [0.0] * D, case["L"], classes, nbshots=case["nbshots"], volume=vol)

@@ -83,6 +83,37 @@ def test_fp32_guard_form_matches_fp64_in_higher_dimensions_and_with_classes(dim,
         assert out[1][3]["maximal"] == 1
 
 
+@pytest.mark.parametrize("dim,L,r0,r1,phi_ref", [
+    (2, [1.0, 1.0], 0.02, 0.025, 0.585),     # reference u2d_r0.02-0.025_s7: 0.58495
+    (3, [1.0, 1.0, 1.0], 0.05, 0.055, 0.40),  # reference u3d_r0.05-0.055_s0: 0.40099
+])
+def test_continuous_radius_law_product_path(dim, L, r0, r1, phi_ref):
+    """Per-dart radii (the reference's RandomRadiusGenerator with a uniform transform): radii in [r0, r1), all
+    distinct, no overlap, no voxel left uncovered for r0, the FP32 form equal to the FP64 form, and the packing
+    fraction of the reference's run within sampling noise."""
+    out = []
+    for form in (_lib.RSAGPU_FORM_FP64, _lib.RSAGPU_FORM_FP32_GUARD):
+        fr = []
+        for seed in range(6):
+            rg = RadiusGenerator.uniform(dim, r0, r1)
+            dom = Domain([0.0] * dim, L, rg.max_radius)
+            algo = Algo(dom, rg, 6000)
+            algo.set_form(form)
+            algo.proceed(40 + seed)
+            assert algo.stats()["maximal"] == 1
+            pos, rad, ph = dom.arrays()
+            assert dom.check() == (0, 0)
+            if seed == 0:
+                out.append((pos, rad))
+                assert np.all(rad >= r0) and np.all(rad < r1) and len(np.unique(rad)) == len(rad)
+                assert O.count_overlaps(dim, [0.0] * dim, L, pos, rad) == 0
+                assert O.uncovered_after_refinement(dim, [0.0] * dim, L, pos, rad, r1, r0, 40) == 0
+            fr.append(sum(O.volume_sphere(dim, x) for x in rad) / float(np.prod(L)))
+        assert abs(np.mean(fr) - phi_ref) < 0.02, fr
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
 def test_product_runs_are_deterministic_per_seed():
     d1, _ = run_product(2, [1.0, 1.0], 0.01, 3)
     d2, _ = run_product(2, [1.0, 1.0], 0.01, 3)

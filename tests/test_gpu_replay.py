@@ -15,10 +15,12 @@ from gpu_helpers import GOLDEN, INDEX, lockstep, sort_spheres
 pytestmark = pytest.mark.gpu
 
 MONO = ["c1_2d_r0.005_s0", "t2d_r0.05_s0", "t3d_r0.05_s0", "k3d_r0.02_s1", "t3d_box3.5_r0.4_s0", "n2d_rect_s7"]
+# continuous radius law (RandomRadiusGenerator, uniform transform): per-dart radii from the reference's stream
+UNIFORM = ["u3d_r0.05-0.055_s0", "u2d_r0.02-0.025_s7", "u2d_r0.01-0.0105_s3"]
 
 
 @pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
-@pytest.mark.parametrize("name", MONO)
+@pytest.mark.parametrize("name", MONO + UNIFORM)
 def test_replay_reproduces_reference_output(name, form):
     case = INDEX[name]
     g = np.load(f"{GOLDEN}/{name}.npz")

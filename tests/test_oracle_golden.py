@@ -30,6 +30,11 @@ def _sorted(pos, rad, ph):
 
 def run_oracle(case):
     D = case["dim"]
+    if "uniform" in case:
+        r0, r1, count, ph = case["uniform"]
+        o = O.Oracle.uniform(D, [0.0] * D, case["L"], r0, r1, count, ph, nbshots=case["nbshots"])
+        o.proceed(case["seed"])
+        return o
     vol = 1.0 if case["volume_mode"] == 1 else float(np.prod(case["L"]))
     o = O.Oracle(D, [0.0] * D, case["L"], [tuple(x) for x in case["classes"]], nbshots=case["nbshots"], volume=vol)
     o.proceed(case["seed"])
@@ -76,6 +81,20 @@ def test_golden_outputs_have_no_overlap_and_are_maximal(name):
     rmax = max(c[0] for c in case["classes"])
     rmin = min(c[0] for c in case["classes"])
     assert O.uncovered_after_refinement(D, inf, sup, g["centers"], g["radii"], rmax, rmin, 40) == 0
+
+
+@pytest.mark.parametrize("name", ["u3d_r0.05-0.055_s0", "u2d_r0.02-0.025_s7", "u2d_r0.01-0.0105_s3"])
+def test_continuous_radius_outputs_are_valid_and_maximal(name):
+    """The reference with a continuous (uniform) radius law: radii in [r_min, r_max), no overlap, and no
+    voxel left uncovered for the smallest radius (the run ends on an empty voxel list)."""
+    case = INDEX[name]
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    D = case["dim"]
+    r0, r1, _, ph = case["uniform"]
+    assert np.all(g["radii"] >= r0) and np.all(g["radii"] < r1) and np.all(g["phases"] == ph)
+    assert len(np.unique(g["radii"])) == len(g["radii"])
+    assert O.count_overlaps(D, [0.0] * D, case["L"], g["centers"], g["radii"]) == 0
+    assert O.uncovered_after_refinement(D, [0.0] * D, case["L"], g["centers"], g["radii"], r1, r0, 40) == 0
 
 
 @pytest.mark.parametrize("name", ["p2d_poly_s3", "p3d_poly_small_s2", "t3d_radius_s0"])
