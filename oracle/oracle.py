@@ -49,6 +49,7 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.ora_create.restype = C.c_void_p
         L.ora_create.argtypes = [C.c_int, _d, _d, C.c_double, C.c_int, _d, _u64, _i32, C.c_double, C.c_int]
+        L.ora_reset_classes.argtypes = [C.c_void_p, C.c_int, _d, _u64, _i32, C.c_double]
         L.ora_create_uniform.restype = C.c_void_p
         L.ora_create_uniform.argtypes = [C.c_int, _d, _d, C.c_double, C.c_double, C.c_uint64, C.c_int, C.c_int]
         L.ora_destroy.argtypes = [C.c_void_p]
@@ -151,6 +152,16 @@ class Oracle:
         if not self._h:
             raise RuntimeError("oracle: invalid configuration")
         return self
+
+    def reset(self, classes, volume=None, exclusion=0.0):
+        """reset_radius_generator with classes (r, phi, phase) on the same domain and spheres."""
+        if volume is None:
+            volume = float(np.prod(self.sup - self.inf))
+        r = np.array([c[0] for c in classes], dtype=np.float64)
+        n = np.array([count_from_fraction(self.dim, c[0], c[1], volume) for c in classes], dtype=np.uint64)
+        ph = np.array([int(c[2]) for c in classes], dtype=np.int32)
+        if lib().ora_reset_classes(self._h, len(classes), _p(r, _d), _p(n, _u64), _p(ph, _i32), exclusion) != 0:
+            raise RuntimeError("Incorrect maximal radius")
 
     def __del__(self):
         if getattr(self, "_h", None):

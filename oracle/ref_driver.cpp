@@ -24,6 +24,12 @@
  * The same run with a continuous radius law: sac_de_billes::RandomRadiusGenerator with the transform
  * x -> r_min + (r_max - r_min) x of a uniform x (radius_generator.hxx:12-38, the uniform law of
  * test/test_random_radius_generator.cpp:13-29), <count> spheres wanted.
+ *
+ *   ref_rsa reiter <dim> <seed> <nbshots> <L_0..L_{D-1}> <r_0> <multiplier> <steps> <out.bin>
+ *
+ * Re-iteration as scripts/main_max_frac.cpp:30-60: a maximal run with radius r_0, then <steps> times the
+ * radius multiplied by <multiplier>, reset_radius_generator and proceed(seed) on the same domain
+ * (rsa_algo::reset_radius_generator, operator_algorithm.ixx:238-250).
  */
 #include <chrono>
 #include <cstdio>
@@ -141,9 +147,57 @@ int run_uniform_radius(int argc, char** argv) {
     return write_spheres<DIM>(domain, out);
 }
 
+template<int DIM>
+int run_reiterate(int argc, char** argv) {
+    // argv: reiter dim seed nbshots L... r0 multiplier steps out
+    int a = 2;
+    size_t seed = std::strtoull(argv[a++], nullptr, 10);
+    int nbshots = std::atoi(argv[a++]);
+    std::array<double, DIM> inf{}, sup{};
+    for (int d = 0; d < DIM; d++) {
+        inf[d] = 0.;
+        sup[d] = std::strtod(argv[a++], nullptr);
+    }
+    double rad = std::strtod(argv[a++], nullptr);
+    const double multiplier = std::strtod(argv[a++], nullptr);
+    const int steps = std::atoi(argv[a++]);
+    std::string out = argv[a++];
+    if (a > argc) return 2;
+    double volume = 1.;
+    for (int d = 0; d < DIM; d++) volume *= (sup[d] - inf[d]);
+    sac_de_billes::RadiusGenerator<DIM> radius_generator(
+        std::vector<std::tuple<double, double, int>>{{rad, 1., 0}}, volume);
+    rsa_domain<DIM> domain(inf, sup, 1, radius_generator.get_max_radius());
+    algorithm::rsa_algo<DIM> algo(domain, radius_generator, nbshots, 10);
+    auto t0 = std::chrono::steady_clock::now();
+    algo.template proceed<1>(seed);
+    for (int j = 0; j < steps; j++) {
+        rad *= multiplier;
+        sac_de_billes::RadiusGenerator<DIM> next(std::vector<std::tuple<double, double, int>>{{rad, 1., 0}}, volume);
+        algo.reset_radius_generator(next);
+        algo.template proceed<1>(seed);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    std::printf("proceed_seconds %.6f\n", std::chrono::duration<double>(t1 - t0).count());
+    return write_spheres<DIM>(domain, out);
+}
+
 } // namespace
 
 int main(int argc, char** argv) {
+    if (argc >= 3 && std::string(argv[1]) == "reiter") {
+        int dim = std::atoi(argv[2]);
+        argv[2] = argv[1];
+        argv++;
+        argc--;
+        switch (dim) {
+        case 2: return run_reiterate<2>(argc, argv);
+        case 3: return run_reiterate<3>(argc, argv);
+        default:
+            std::fprintf(stderr, "dim %d not built\n", dim);
+            return 2;
+        }
+    }
     if (argc >= 3 && std::string(argv[1]) == "runu") {
         int dim = std::atoi(argv[2]);
         argv[2] = argv[1];

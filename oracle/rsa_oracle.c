@@ -514,6 +514,42 @@ rsa_oracle* ora_create_uniform(int dim, const double* inf, const double* sup, do
     return o;
 }
 
+/* rsa_algo::reset_radius_generator (operator_algorithm.ixx:238-250): a new class list on the same domain and
+ * spheres; the algorithm's r_max stays the larger of the two (m_r_max), which the next voxel lattice uses. */
+int ora_reset_classes(rsa_oracle* o, int n_classes, const double* radii, const uint64_t* counts,
+    const int* phases, double exclusion_distance) {
+    if (!o || n_classes < 1) return -1;
+    double* r = (double*)malloc(sizeof(double) * n_classes);
+    uint64_t* n = (uint64_t*)malloc(sizeof(uint64_t) * n_classes);
+    int* ph = (int*)malloc(sizeof(int) * n_classes);
+    for (int i = 0; i < n_classes; i++) {
+        r[i] = radii[i];
+        n[i] = counts[i];
+        ph[i] = phases[i];
+    }
+    for (int i = 1; i < n_classes; i++) {
+        for (int j = i; j > 0 && r[j] > r[j - 1]; j--) {
+            double tr = r[j]; r[j] = r[j - 1]; r[j - 1] = tr;
+            uint64_t tn = n[j]; n[j] = n[j - 1]; n[j - 1] = tn;
+            int tp = ph[j]; ph[j] = ph[j - 1]; ph[j - 1] = tp;
+        }
+    }
+    for (int i = 0; i < n_classes; i++) r[0] += 0.5 * exclusion_distance;
+    if (r[0] > o->r_max) {
+        free(r); free(n); free(ph);
+        return -2; /* runtime_error("Incorrect maximal radius") */
+    }
+    free(o->cls_r); free(o->cls_n); free(o->cls_phase);
+    o->cls_r = r;
+    o->cls_n = n;
+    o->cls_phase = ph;
+    o->k = n_classes;
+    o->cls_idx = 0;
+    o->r_min = r[n_classes - 1];
+    o->uniform_radius = 0;
+    return 0;
+}
+
 void ora_destroy(rsa_oracle* o) {
     if (!o) return;
     store_free(&o->st);

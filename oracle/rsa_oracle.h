@@ -46,6 +46,11 @@ void ora_destroy(rsa_oracle* o);
 rsa_oracle* ora_create_uniform(int dim, const double* inf, const double* sup, double r_min, double r_max,
     uint64_t count, int phase, int nbshots);
 
+/* rsa_algo::reset_radius_generator (operator_algorithm.ixx:238-250): new classes, same spheres; r_max stays the
+ * larger one.  Returns -2 for a larger maximal radius (the reference throws). */
+int ora_reset_classes(rsa_oracle* o, int n_classes, const double* radii, const uint64_t* counts,
+    const int* phases, double exclusion_distance);
+
 /* uint64(volume * phi / v_D(r)) as compute_desired_radius_nb_phase (radius_generator.ixx:71-86). */
 uint64_t ora_count_from_fraction(int dim, double r, double phi, double volume);
 /* v_D(r) as sphereTools::volumeSphere (auxiliary/Geometry/Sphere.ixx:30-57). */

@@ -1164,6 +1164,20 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
     }
 }
 
+// regrid: spheres put back into a rebuilt grid enter it as accepted candidates (k_commit); their cells
+__global__ void k_locate(Grid<D> g, Geo<D> geo, CandArgs c) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    double x[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
+    int32_t k[D];
+    cell_of<D>(g, geo, x, k);
+    c.cell[i] = cell_index<D>(g, k);
+    c.state[i] = ST_ACCEPTED;
+    c.alive[i] = i;
+}
+
 // ------------------------------------------------------------------------------------------------
 // validators (operator_check_cell.ixx:8-78, rsa_data_storage.ixx:216-243) and reductions
 // ------------------------------------------------------------------------------------------------
@@ -1428,6 +1442,12 @@ void op_refine_write(const RefineArgs& a, cudaStream_t s) {
     count_launch();
 }
 
+void op_locate(const GridArgs& ga, const CandArgs& c, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_locate<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    count_launch();
+}
+
 void op_check(const GridArgs& ga, unsigned long long* overlaps, unsigned long long* misplaced, cudaStream_t s) {
     k_check<<<nblocks(ga.ncells, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), overlaps, misplaced);
     count_launch();
@@ -1464,6 +1484,7 @@ const DimOps kOps = {
     op_check,
     op_volume_partials,
     op_extract_write,
+    op_locate,
     CHILDREN,
     MASK_WORDS,
     op_batch_table_bytes,

@@ -181,6 +181,8 @@ struct DimOps {
     void (*volume_partials)(const GridArgs& g, double unit_volume, double* partials, int nblocks, cudaStream_t s);
     void (*extract_write)(const GridArgs& g, const uint64_t* block_offsets, double* pos, double* rad,
                           int32_t* phase, cudaStream_t s);
+    // regrid: cell of each of c.n spheres in c.pos, state ACCEPTED, alive list 0..n-1 (then commit)
+    void (*locate)(const GridArgs& g, const CandArgs& c, cudaStream_t s);
     int children;      // 2^D
     int mask_words;    // 32-bit words of child mask per voxel
     // batched instances (block = threads per block, from the autotuner)

@@ -129,6 +129,7 @@ struct rsagpu_algo {
     rsagpu_domain* dom = nullptr;
     rsagpu_radgen rg;
     int nbshots = 6000;
+    double rmax_algo = 0;  // m_r_max: the largest r_max of the radius generators so far
     const DimOps* ops = nullptr;
     cudaStream_t stream = nullptr;
     // voxels
@@ -441,6 +442,48 @@ CandArgs cand_args(rsagpu_algo* A, uint32_t n) {
     return c;
 }
 
+// Rebuilds the domain's grid for a smaller minimal radius with the placed spheres kept: they are extracted on
+// the device, the grid is rebuilt (cells for rmin, stencil for rmax), and they re-enter it as accepted
+// candidates through the commit kernel.  Spheres of radius >= rmin are more than 2 rmin apart, so each
+// new cell still holds at most one of them (checked by the commit kernel).
+void regrid(rsagpu_algo* A, double rmin, double rmax) {
+    rsagpu_domain* dom = A->dom;
+    const GridArgs old = dom->grid.a;
+    const int64_t nwords = (old.ncells + 31) / 32;
+    const uint64_t nb = (nwords + OCC_BLOCK - 1) / OCC_BLOCK;
+    uint32_t* counts = dalloc<uint32_t>(nb);
+    uint64_t* offs = dalloc<uint64_t>(nb + 1);
+    launch_occ_block_counts(old.occ, nwords, counts, dom->stream);
+    launch_scan_blocks(counts, offs, nb, nullptr, dom->stream);
+    uint64_t total = 0;
+    CK(cudaMemcpyAsync(&total, offs + nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, dom->stream));
+    CK(cudaStreamSynchronize(dom->stream));
+    ensure_cand(A, total);
+    CandArgs c = cand_args(A, (uint32_t)total);
+    c.lazy = 0;
+    if (total) A->ops->extract_write(old, offs, c.pos, c.rad, c.phase, dom->stream);
+    CK(cudaStreamSynchronize(dom->stream));
+    dfree(counts);
+    dfree(offs);
+    build_grid(dom, rmin, rmax);
+    dom->grid.a.mono = 0;
+    dom->grid.a.rmono = 0;
+    A->heads_dirty = false;
+    if (total == 0) return;
+    c.head = dom->grid.head;  // the new grid's candidate lists (the old ones were released)
+    c.cocc = dom->grid.cocc;
+    CK(cudaMemsetAsync(c.counters, 0, (COUNTERS + MAX_SETTLE + 1) * sizeof(uint32_t), A->stream));
+    A->ops->locate(dom->grid.a, c, A->stream);
+    const uint32_t n32 = (uint32_t)total;
+    CK(cudaMemcpyAsync(c.counters, &n32, sizeof(uint32_t), cudaMemcpyHostToDevice, A->stream));
+    A->ops->commit(dom->grid.a, c, A->stream);
+    CK(cudaMemcpyAsync(A->h_counters, c.counters, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
+    CK(cudaStreamSynchronize(A->stream));
+    if (A->h_counters[2] & ERR_DOUBLE_OCCUPANCY) raise(RSAGPU_ERR_INVARIANT, "regrid: two centres in one cell");
+    if (A->h_counters[1] != total) raise(RSAGPU_ERR_INVARIANT, "regrid: %u of %llu spheres put back",
+                                         A->h_counters[1], (unsigned long long)total);
+}
+
 void ensure_vox(rsagpu_algo* A, int which, uint64_t n) {
     const int D = A->dom->dim;
     if (n <= A->vox_cap[which]) return;
@@ -473,7 +516,9 @@ void begin(rsagpu_algo* A) {
     const int D = A->dom->dim;
     // list_of_voxels(origin, L, r_max + r_min): n_d = 1 + int(sqrt(D) L_d / diag), len_d = L_d / n_d
     // (list_of_voxels.ixx:11-28, 192-211)
-    const double diag = A->rg.rmax() + A->rg.rmin();
+    // the algorithm's r_max is the largest over its radius generators (m_r_max, operator_algorithm.ixx:89-90,
+    // 246): after a reset to smaller radii the lattice still uses the first one
+    const double diag = A->rmax_algo + A->rg.rmin();
     uint64_t V = 1;
     for (int d = 0; d < D; d++) {
         A->nvox0[d] = 1 + (int)(std::sqrt((double)D) * A->dom->L[d] / diag);
@@ -1260,6 +1305,7 @@ int rsagpu_algo_create(rsagpu_domain* dom, const rsagpu_radgen* rg, int nbshots,
             A->rg = *rg;
             A->rg.idx = 0;
             A->nbshots = nbshots;
+            A->rmax_algo = rg->rmax();
             A->ops = dim_ops(dom->dim);
             if (!A->ops) raise(RSAGPU_ERR_ARG, "dimension not built");
             CK(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking));
@@ -1384,8 +1430,10 @@ int rsagpu_algo_reset_radgen(rsagpu_algo* algo, const rsagpu_radgen* rg) {
         if (!algo || !rg) raise(RSAGPU_ERR_ARG, "null argument");
         // operator_algorithm.ixx:238-250
         if (algo->rg.rmax() < rg->rmax()) raise(RSAGPU_ERR_ARG, "Incorrect maximal radius");
-        if (rg->rmin() < algo->dom->grid.rmin)
-            raise(RSAGPU_ERR_STATE, "a smaller minimal radius than the grid's needs a regrid (not built)");
+        set_device(algo->dom);
+        // a smaller minimal radius needs smaller cells (one centre per cell): regrid, keeping the spheres
+        if (rg->rmin() < algo->dom->grid.rmin) regrid(algo, rg->rmin(), algo->dom->grid.rmax);
+        algo->rmax_algo = std::max(algo->rmax_algo, rg->rmax());
         algo->rg = *rg;
         algo->rg.idx = 0;
         algo->begun = false;

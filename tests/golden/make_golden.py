@@ -16,6 +16,7 @@ import json
 import os
 import re
 import subprocess
+import tempfile
 import sys
 
 import numpy as np
@@ -61,6 +62,15 @@ UNIFORM_CASES = {
 }
 
 
+# re-iteration (scripts/main_max_frac.cpp:30-60): a maximal run with r_0, then <steps> runs with the radius
+# multiplied by <multiplier>, reset_radius_generator and proceed(seed) on the same domain:
+# name -> (dim, seed, nbshots, L, r_0, multiplier, steps)
+REITER_CASES = {
+    "r2d_r0.02x0.7_s1": (2, 1, 6000, [1.0, 1.0], 0.02, 0.7, 3),
+    "r3d_r0.05x0.8_s2": (3, 2, 6000, [1.0, 1.0, 1.0], 0.05, 0.8, 2),
+}
+
+
 def parse_trace(log: str):
     shots = [int(m.group(1)) for m in re.finditer(r"--> Miss rate = .*?Nb shots = (\d+) ; Nb miss", log)]
     miss = [int(m.group(1)) for m in re.finditer(r"--> Miss rate = .*?Nb miss =\s+(\d+)", log)]
@@ -86,16 +96,22 @@ def main():
     jobs = [(name, spec, None) for name, spec in CASES.items()]
     jobs += [(name, (dim, seed, nbshots, 0, L, []), (r0, r1, count, ph))
              for name, (dim, seed, nbshots, L, r0, r1, count, ph) in UNIFORM_CASES.items()]
+    jobs += [(name, (dim, seed, nbshots, 0, L, [(r0, 1.0, 0)]), ("reiter", mult, steps))
+             for name, (dim, seed, nbshots, L, r0, mult, steps) in REITER_CASES.items()]
+    tmp = tempfile.mkdtemp(prefix="rsa_golden_")
     for name, (dim, seed, nbshots, vmode, L, classes), uniform in jobs:
         if args.only and args.only != name:
             continue
-        out = os.path.join(ROOT, "_work", f"golden_{name}.bin")
-        os.makedirs(os.path.dirname(out), exist_ok=True)
+        out = os.path.join(tmp, f"golden_{name}.bin")
         if uniform is None:
             cmd = [ref, "run", str(dim), str(seed), str(nbshots), str(vmode)] + [repr(x) for x in L]
             cmd += [str(len(classes))]
             for r, phi, ph in classes:
                 cmd += [repr(r), repr(phi), str(ph)]
+        elif uniform[0] == "reiter":
+            _, mult, steps = uniform
+            cmd = [ref, "reiter", str(dim), str(seed), str(nbshots)] + [repr(x) for x in L]
+            cmd += [repr(classes[0][0]), repr(mult), str(steps)]
         else:
             r0, r1, count, ph = uniform
             cmd = [ref, "runu", str(dim), str(seed), str(nbshots)] + [repr(x) for x in L]
@@ -113,7 +129,9 @@ def main():
         index[name] = dict(dim=dim, seed=seed, nbshots=nbshots, volume_mode=vmode, L=L,
                            classes=[list(x) for x in classes], n_spheres=int(len(r)),
                            volume_of_spheres=vol, rounds=int(len(shots)), ref_seconds_8threads=secs)
-        if uniform is not None:
+        if uniform is not None and uniform[0] == "reiter":
+            index[name]["reiterate"] = [uniform[1], uniform[2]]
+        elif uniform is not None:
             index[name]["uniform"] = list(uniform)
         print(name, len(r), vol, len(shots), f"{secs:.3f}s")
     with open(index_path, "w") as f:

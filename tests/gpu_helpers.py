@@ -52,6 +52,11 @@ def lockstep(case, seed, cap_exact=False, check_voxels=True, max_rounds=100000, 
     """Drives the oracle and the GPU with the reference's own candidate stream; asserts equal decisions
     every round and equal voxel sets after every refinement.  Returns (oracle, algo, dom, rounds)."""
     ora, algo, dom = make_pair(case, cap_exact, form)
+    return (ora, algo, dom) + (drive(ora, algo, seed, check_voxels, max_rounds),)
+
+
+def drive(ora, algo, seed, check_voxels=True, max_rounds=100000):
+    """One proceed of both sides in lockstep (see lockstep); returns the number of rounds."""
     ora.begin(seed)
     algo.begin()
     rounds = 0
@@ -79,4 +84,4 @@ def lockstep(case, seed, cap_exact=False, check_voxels=True, max_rounds=100000, 
         rounds += 1
         if done_o:
             break
-    return ora, algo, dom, rounds
+    return rounds

@@ -6,7 +6,7 @@ import pytest
 from oracle import oracle as O
 from rsa_mpi_gb300 import _lib
 from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator
-from gpu_helpers import INDEX, sort_voxels
+from gpu_helpers import INDEX, sort_spheres, sort_voxels
 
 pytestmark = pytest.mark.gpu
 
@@ -112,6 +112,37 @@ def test_continuous_radius_law_product_path(dim, L, r0, r1, phi_ref):
         assert abs(np.mean(fr) - phi_ref) < 0.02, fr
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("dim,L,radii", [
+    (2, [1.0, 1.0], (0.02, 0.012, 0.006)),
+    (3, [1.0, 1.0, 1.0], (0.05, 0.03)),
+])
+def test_reiteration_product_path(dim, L, radii):
+    """reset_radius_generator to smaller radii on the same domain, proceeding after each reset: the grid is
+    rebuilt for the new radius, the old spheres stay, the result is maximal for the last radius, no overlap,
+    and the FP32 form places the same spheres as the FP64 form."""
+    out = []
+    vol = float(np.prod(L))
+    for form in (_lib.RSAGPU_FORM_FP64, _lib.RSAGPU_FORM_FP32_GUARD):
+        dom = Domain([0.0] * dim, L, radii[0])
+        algo = Algo(dom, RadiusGenerator(dim, [(radii[0], 1.0, 0)], volume=vol), 6000)
+        algo.set_form(form)
+        n_prev = 0
+        for i, r in enumerate(radii):
+            if i:
+                algo.reset_radius_generator(RadiusGenerator(dim, [(r, 1.0, 0)], volume=vol))
+            algo.proceed(11 + i)
+            assert algo.stats()["maximal"] == 1
+            pos, rad, ph = dom.arrays()
+            assert len(rad) > n_prev and np.count_nonzero(rad == r) == len(rad) - n_prev
+            n_prev = len(rad)
+            assert dom.check() == (0, 0)
+        assert O.count_overlaps(dim, [0.0] * dim, L, pos, rad) == 0
+        assert O.uncovered_after_refinement(dim, [0.0] * dim, L, pos, rad, radii[0], radii[-1], 40) == 0
+        out.append(sort_spheres(pos, rad, ph))
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_product_runs_are_deterministic_per_seed():

@@ -10,7 +10,8 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from gpu_helpers import GOLDEN, INDEX, lockstep, sort_spheres
+from gpu_helpers import GOLDEN, INDEX, drive, lockstep, make_pair, sort_spheres
+from rsa_mpi_gb300.sampler import RadiusGenerator
 
 pytestmark = pytest.mark.gpu
 
@@ -49,3 +50,33 @@ def test_replay_polydisperse_exact_cap(name, form):
     vol = 1.0 if case["volume_mode"] == 1 else float(np.prod(case["L"]))
     counts = [O.count_from_fraction(case["dim"], r, phi, vol) for r, phi, _ in case["classes"]]
     np.testing.assert_array_equal(np.bincount(fg, minlength=len(counts)), counts)
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
+@pytest.mark.parametrize("name", ["r2d_r0.02x0.7_s1", "r3d_r0.05x0.8_s2"])
+def test_replay_reiteration_reproduces_reference_output(name, form):
+    """reset_radius_generator with a smaller radius on the same domain, then proceed again: the grid is
+    rebuilt for the new radius, the voxel lattice keeps the algorithm's largest r_max, and after every stage
+    the sphere sets agree; the final set equals the reference's own output."""
+    case = INDEX[name]
+    g = np.load(f"{GOLDEN}/{name}.npz")
+    mult, steps = case["reiterate"]
+    rad = case["classes"][0][0]
+    ora, algo, dom = make_pair(case, form=form)
+    D = case["dim"]
+    vol = float(np.prod(case["L"]))
+    for stage in range(steps + 1):
+        if stage:
+            rad *= mult
+            ora.reset([(rad, 1.0, 0)], volume=vol)
+            algo.reset_radius_generator(RadiusGenerator(D, [(rad, 1.0, 0)], volume=vol))
+        drive(ora, algo, case["seed"])
+        po, ro, fo = sort_spheres(*ora.spheres())
+        pg, rg, fg = sort_spheres(*dom.arrays())
+        np.testing.assert_array_equal(po, pg)
+        np.testing.assert_array_equal(ro, rg)
+        assert len(algo.voxels()[0]) == 0
+    np.testing.assert_array_equal(pg, g["centers"])
+    np.testing.assert_array_equal(rg, g["radii"])
+    np.testing.assert_array_equal(fg, g["phases"])
+    assert dom.check() == (0, 0)

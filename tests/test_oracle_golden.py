@@ -30,6 +30,16 @@ def _sorted(pos, rad, ph):
 
 def run_oracle(case):
     D = case["dim"]
+    if "reiterate" in case:  # r_0, then steps runs with the radius multiplied, on the same domain
+        mult, steps = case["reiterate"]
+        rad = case["classes"][0][0]
+        o = O.Oracle(D, [0.0] * D, case["L"], [(rad, 1.0, 0)], nbshots=case["nbshots"])
+        o.proceed(case["seed"])
+        for _ in range(steps):
+            rad *= mult
+            o.reset([(rad, 1.0, 0)])
+            o.proceed(case["seed"])
+        return o
     if "uniform" in case:
         r0, r1, count, ph = case["uniform"]
         o = O.Oracle.uniform(D, [0.0] * D, case["L"], r0, r1, count, ph, nbshots=case["nbshots"])
@@ -56,6 +66,8 @@ def test_full_run_matches_reference(name):
     np.testing.assert_array_equal(pos, g["centers"])
     np.testing.assert_array_equal(rad, g["radii"])
     np.testing.assert_array_equal(ph, g["phases"])
+    if "reiterate" in case:
+        return
     tr = o.trace()
     np.testing.assert_array_equal(tr["shots"].astype(np.int64), g["shots"])
     np.testing.assert_array_equal((tr["shots"] - tr["new"]).astype(np.int64), g["miss"])
