@@ -2,8 +2,9 @@
 // (MarcJos/RSA_MPI include/user_interface.hxx:13-124), over the C ABI of include/rsagpu.h.
 //
 // Header-only; link with librsagpu.so.  Errors are thrown as std::runtime_error, as in the reference.
-// Differences: the spheres live on the GPU of the calling thread; paraview() is not provided here
-// (rsa_mpi_gb300.writers writes the reference's files from extracted spheres).
+// Differences: the spheres live on the GPU of the calling thread.  extract_spheres() and paraview() list them
+// Real cell by Real cell in the reference's cell-grid order (rsa_gpu_output::reference_cell_order); within
+// one cell, spheres accepted in the same round can come in another order than the reference's.
 #pragma once
 
 #include <array>
@@ -15,6 +16,7 @@
 #include <vector>
 
 #include "../rsagpu.h"
+#include "writers.hxx"
 
 namespace user_interface {
 
@@ -40,7 +42,7 @@ class rsa_domain {
 public:
     // rsa_domain(global_inf, global_sup, a_rad) (user_interface.hxx:24-25)
     rsa_domain(const Point<DIM>& global_inf, const Point<DIM>& global_sup, const double a_rad)
-        : inf_(global_inf), sup_(global_sup) {
+        : inf_(global_inf), sup_(global_sup), rad_(a_rad) {
         rsagpu_domain* d = nullptr;
         detail::check(rsagpu_domain_create(DIM, inf_.data(), sup_.data(), a_rad, &d));
         ptr_ = std::shared_ptr<rsagpu_domain>(d, [](rsagpu_domain* p) { rsagpu_domain_destroy(p); });
@@ -58,24 +60,50 @@ public:
         return v;
     }
     void domain_log() const {}
+    // extract_spheres (rsa_grid.ixx:88-98): the spheres in the reference's Real-cell order
     std::vector<rsa_sphere<DIM>> extract_spheres() const {
-        uint64_t n = 0;
-        detail::check(rsagpu_domain_extract(ptr_.get(), nullptr, nullptr, nullptr, 0, &n));
-        std::vector<double> c(n * DIM), r(n);
-        std::vector<int> ph(n);
-        detail::check(rsagpu_domain_extract(ptr_.get(), c.data(), r.data(), ph.data(), n, &n));
-        std::vector<rsa_sphere<DIM>> out(n);
-        for (uint64_t i = 0; i < n; i++) {
+        std::vector<double> c, r;
+        std::vector<int> ph;
+        extract_arrays(c, r, ph);
+        std::vector<rsa_sphere<DIM>> out(r.size());
+        for (size_t i = 0; i < r.size(); i++) {
             for (int d = 0; d < DIM; d++) out[i].center[d] = c[i * DIM + d];
             out[i].radius = r[i];
             out[i].phase = ph[i];
         }
         return out;
     }
+    // paraview() -> rsa_paraview::paraview(domain, "ParaviewOutput") (operator_paraview.hxx:35,
+    // operator_paraview.ixx:69-120)
+    void paraview() const {
+        std::vector<double> c, r;
+        std::vector<int> ph;
+        extract_arrays(c, r, ph);
+        rsa_gpu_output::paraview<DIM>("ParaviewOutput", c.data(), r.data(), ph.data(), r.size());
+    }
+    // centres (n x DIM), radii and phases copied off the GPU, in the reference's Real-cell order
+    void extract_arrays(std::vector<double>& c, std::vector<double>& r, std::vector<int>& ph) const {
+        uint64_t n = 0;
+        detail::check(rsagpu_domain_extract(ptr_.get(), nullptr, nullptr, nullptr, 0, &n));
+        std::vector<double> c0(n * DIM), r0(n);
+        std::vector<int> ph0(n);
+        detail::check(rsagpu_domain_extract(ptr_.get(), c0.data(), r0.data(), ph0.data(), n, &n));
+        const auto order = rsa_gpu_output::reference_cell_order<DIM>(c0.data(), n, inf_, sup_, rad_);
+        c.resize(n * DIM);
+        r.resize(n);
+        ph.resize(n);
+        for (uint64_t i = 0; i < n; i++) {
+            const size_t j = order[i];
+            for (int d = 0; d < DIM; d++) c[i * DIM + d] = c0[j * DIM + d];
+            r[i] = r0[j];
+            ph[i] = ph0[j];
+        }
+    }
     rsagpu_domain* handle() const { return ptr_.get(); }
 
 private:
     Point<DIM> inf_, sup_;
+    double rad_;
     std::shared_ptr<rsagpu_domain> ptr_;
 };
 
@@ -145,6 +173,10 @@ public:
     void reset_radius_generator(RadiusGenerator<DIM>& a_radius_generator) {
         detail::check(rsagpu_algo_reset_radgen(ptr_.get(), a_radius_generator.handle()));
     }
+    // not in the reference: the arithmetic form (RSAGPU_FORM_FP64 or RSAGPU_FORM_FP32_GUARD) and schedule
+    void set_form(int form, int schedule = RSAGPU_SCHEDULE_HEURISTIC) {
+        detail::check(rsagpu_algo_set_form(ptr_.get(), form, schedule));
+    }
 
 private:
     rsa_domain<DIM>* domain_;
@@ -157,7 +189,6 @@ template <int DIM>
 std::vector<rsa_sphere<DIM>> throw_spheres(Point<DIM> L,
                                            std::vector<std::tuple<double, double, int>> desired_radius_volumeFraction_phase,
                                            size_t seed, bool write_paraview) {
-    (void)write_paraview;
     Point<DIM> inf{};
     RadiusGenerator<DIM> rg(desired_radius_volumeFraction_phase, 1.0, 0.0);
     rsa_domain<DIM> domain(inf, L, rg.get_max_radius());
@@ -165,6 +196,7 @@ std::vector<rsa_sphere<DIM>> throw_spheres(Point<DIM> L,
         rsa_algo<DIM> algo(domain, rg, 6000);
         algo.proceed(seed);
     }
+    if (write_paraview) domain.paraview();
     return domain.extract_spheres();
 }
 

@@ -30,6 +30,11 @@
  * Re-iteration as scripts/main_max_frac.cpp:30-60: a maximal run with radius r_0, then <steps> times the
  * radius multiplied by <multiplier>, reset_radius_generator and proceed(seed) on the same domain
  * (rsa_algo::reset_radius_generator, operator_algorithm.ixx:238-250).
+ *
+ * With RSA_REF_OUTPUTS=<dir> in the environment, every mode also writes the reference's own output files of
+ * the final spheres into <dir>: ParaView (rsa_paraview::paraview, operator_paraview.ixx:69-120) under <dir>/pv,
+ * legacy VTK (rsa_data_storage::write_spheres of the Real cells' data, rsa_data_storage.ixx:166-207) as
+ * <dir>/spheres.vtk and, in 3D, XYZ (plugin/write_xyz.hpp:79-98) as <dir>/spheres.xyz.
  */
 #include <chrono>
 #include <cstdio>
@@ -40,6 +45,8 @@
 #include <rsa_domain.hxx>
 #include <radius_generator.hxx>
 #include <operator_algorithm.hxx>
+#include <operator_paraview.hxx>
+#include <write_xyz.hpp>
 
 namespace {
 
@@ -94,6 +101,16 @@ int run(int argc, char** argv) {
     std::fclose(f);
     std::printf("spheres %lld volume_of_spheres %.17g\n", (long long)n,
         domain.compute_total_volume_of_spheres());
+    if (const char* dir = std::getenv("RSA_REF_OUTPUTS")) {
+        const std::string d = dir;
+        rsa_paraview::paraview(domain, d + "/pv");
+        auto data = domain.get_grid().template extract_data<TypeCell::Real>();
+        data.write_spheres(d + "/spheres.vtk");
+        if constexpr (DIM == 3) {
+            auto sup = domain.get_sup();
+            write_xyz<DIM>(d + "/spheres.xyz", data, sup);
+        }
+    }
     return 0;
 }
 
@@ -116,6 +133,16 @@ int write_spheres(rsa_domain<DIM>& domain, const std::string& out) {
     std::fclose(f);
     std::printf("spheres %lld volume_of_spheres %.17g\n", (long long)n,
         domain.compute_total_volume_of_spheres());
+    if (const char* dir = std::getenv("RSA_REF_OUTPUTS")) {
+        const std::string d = dir;
+        rsa_paraview::paraview(domain, d + "/pv");
+        auto data = domain.get_grid().template extract_data<TypeCell::Real>();
+        data.write_spheres(d + "/spheres.vtk");
+        if constexpr (DIM == 3) {
+            auto sup = domain.get_sup();
+            write_xyz<DIM>(d + "/spheres.xyz", data, sup);
+        }
+    }
     return 0;
 }
 

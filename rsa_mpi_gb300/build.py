@@ -17,6 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "librsagpu.so")
+CLI = os.path.join(OUT, "rsa")  # the command-line sampler (csrc/rsa_cli.cpp), linked against LIB
 DIMS = (2, 3, 4, 5, 6, 7)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction anywhere; the FP64 decisions also use explicit _rn intrinsics.
@@ -34,15 +35,38 @@ def _sources():
         os.path.join(ROOT, "include", "rsagpu.h")]
 
 
+def _cli_sources():
+    inc = os.path.join(ROOT, "include", "rsa_gpu")
+    return [os.path.join(CSRC, "rsa_cli.cpp"), LIB] + [os.path.join(inc, f) for f in os.listdir(inc)]
+
+
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
     t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(s) <= t for s in _sources())
+    if not all(os.path.getmtime(s) <= t for s in _sources()):
+        return False
+    return all(os.path.getmtime(s) <= os.path.getmtime(CLI) for s in _cli_sources())
+
+
+def build_cli() -> str:
+    """g++ build of the command-line sampler; the library is found next to it at run time."""
+    tmp = CLI + ".tmp"
+    cmd = ["g++", "-std=c++17", "-O2", f"-I{os.path.join(ROOT, 'include')}", os.path.join(CSRC, "rsa_cli.cpp"),
+           "-o", tmp, f"-L{OUT}", "-lrsagpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed for rsa_cli.cpp:\n{r.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and up_to_date():
+        return LIB
+    lib_fresh = os.path.exists(LIB) and all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in _sources())
+    if not force and lib_fresh:
+        build_cli()
         return LIB
     os.makedirs(OUT, exist_ok=True)
     jobs = []
@@ -71,6 +95,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
 
 

@@ -64,10 +64,13 @@ def _make(dim: int):
             """Return the total volume of the (global) cuboid."""
             return self._d.total_volume()
 
+        def _ordered(self):
+            d = self._d
+            return writers.reference_order(*d.arrays(), d.inf, d.sup, d.rad_max)
+
         def paraview(self):
             """Print paraview output (rsa_paraview::paraview: a .pvtp and one .vtp)."""
-            pos, rad, ph = self._d.arrays()
-            writers.write_paraview("ParaviewOutput", pos, rad, ph)
+            writers.write_paraview("ParaviewOutput", *self._ordered())
 
         def compute_total_volume_of_spheres(self):
             """Compute the cumulated volume of all spheres inside the whole domains."""
@@ -75,7 +78,7 @@ def _make(dim: int):
 
         def extract_spheres(self):
             """return list of spheres inside the domain"""
-            pos, rad, ph = self._d.arrays()
+            pos, rad, ph = self._ordered()
             return [sphere(list(p), r, f) for p, r, f in zip(pos.tolist(), rad.tolist(), ph.tolist())]
 
         def extract_arrays(self):
@@ -133,7 +136,7 @@ def _make(dim: int):
         algo = Algo(dom, rg, 6000)
         algo.proceed(int(seed))
         algo.close()
-        pos, rad, ph = dom.arrays()
+        pos, rad, ph = writers.reference_order(*dom.arrays(), dom.inf, dom.sup, dom.rad_max)
         if write_paraview:
             writers.write_paraview("ParaviewOutput", pos, rad, ph)
         out = [sphere(list(p), r, f) for p, r, f in zip(pos.tolist(), rad.tolist(), ph.tolist())]

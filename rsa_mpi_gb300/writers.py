@@ -1,10 +1,14 @@
 """Output files of the reference, written from sphere arrays copied off the GPU.
 
-Formats follow the reference's writers byte for byte in layout (numbers are
-printed like a default-precision C++ ostream, 6 significant digits):
-  - ParaView .pvtp + .vtp pieces   include/operator_paraview.ixx:12-129
+Formats follow the reference's writers byte for byte (numbers are printed like a
+default-precision C++ ostream, 6 significant digits); the same spheres in the
+same order give the same bytes:
+  - ParaView .pvtp + .vtp pieces   include/operator_paraview.ixx:12-120
   - legacy VTK unstructured grid   include/rsa_data_storage.ixx:166-207 (write_spheres)
   - XYZ                            plugin/write_xyz.hpp:79-98
+The reference lists spheres Real cell by Real cell (reference_order gives that
+order for spheres extracted from the GPU; within one cell the GPU's order is
+kept).  include/rsa_gpu/writers.hxx is the same set of writers in C++.
 """
 from __future__ import annotations
 
@@ -19,6 +23,31 @@ def _g(x) -> str:
     """operator<<(double) with the default precision 6."""
     s = f"{float(x):.6g}"
     return s
+
+
+def reference_cell_keys(pos: np.ndarray, inf, sup, rad: float) -> np.ndarray:
+    """Real-cell index of each centre in the reference's cell grid for a domain [inf, sup] of radius rad, one
+    ghost layer: edge L_d / int(L_d / (2 rad)), shift inf_d - edge, x fastest (rsa_grid_traversal::define,
+    rsa_grid_traversal.ixx:11-28; compute_cell_idx, :373-382)."""
+    pos = np.asarray(pos, dtype=np.float64)
+    key = np.zeros(len(pos), dtype=np.uint64)
+    for d in reversed(range(pos.shape[1])):
+        width = float(sup[d]) - float(inf[d])
+        inside = int(width / (rad * 2))
+        if inside == 0:
+            raise RuntimeError("Too small domain wrt ghost layer")
+        edge = width / inside
+        shift = float(inf[d]) - 1 * edge
+        ijk = ((pos[:, d] - shift) * (1.0 / edge)).astype(np.int64)  # truncation, as the int64 conversion
+        key = key * np.uint64(inside + 2) + ijk.astype(np.uint64)
+    return key
+
+
+def reference_order(pos, rad, phase, inf, sup, rad_max):
+    """The spheres reordered Real cell by Real cell as the reference lists them (apply_on_cells<Real> over
+    build_real_traversal, rsa_grid_traversal.ixx:216-223); stable within a cell."""
+    order = np.argsort(reference_cell_keys(pos, inf, sup, rad_max), kind="stable")
+    return pos[order], rad[order], phase[order]
 
 
 def write_paraview(a_name: str, pos: np.ndarray, rad: np.ndarray, phase: np.ndarray, rank: int = 0,

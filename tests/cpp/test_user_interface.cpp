@@ -36,5 +36,8 @@ int main() {
     if (us.size() < 600 || us.size() > 760) return 4;
     for (const auto& s : us)
         if (s.radius < 0.05 || s.radius >= 0.055) return 5;
+    // output files in the working directory: ParaviewOutput/rsa_mpi_0.pvtp and its piece
+    ud.paraview();
+    std::printf("paraview written\n");
     return 0;
 }

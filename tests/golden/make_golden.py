@@ -52,6 +52,10 @@ CASES = {
     "n2d_rect_s7": (2, 7, 500, 0, [1.3, 0.7], [(0.02, 1.0, 0)]),
 }
 
+# cases whose reference output files (ParaView, legacy VTK, XYZ) are kept under writers/<name>/, with the
+# spheres in the reference's own extraction order (Real cells in traversal order) as writers/<name>/order.npz
+WRITER_CASES = ["t2d_r0.05_s0", "t3d_r0.05_s0", "t3d_radius_s0"]
+
 # continuous radius law (sac_de_billes::RandomRadiusGenerator, radius = r_min + (r_max - r_min) x):
 # name -> (dim, seed, nbshots, L, r_min, r_max, count, phase); count 10^16 runs to maximality
 UNIFORM_CASES = {
@@ -118,8 +122,15 @@ def main():
             cmd += [repr(r0), repr(r1), str(count), str(ph)]
         cmd += [out]
         env = dict(os.environ, OMP_NUM_THREADS="8")
+        env.pop("RSA_REF_OUTPUTS", None)
+        wdir = os.path.join(HERE, "writers", name)
+        if name in WRITER_CASES:
+            os.makedirs(wdir, exist_ok=True)
+            env["RSA_REF_OUTPUTS"] = wdir
         log = subprocess.run(cmd, check=True, capture_output=True, text=True, env=env).stdout
         c, r, p = O.read_ref_spheres(out)
+        if name in WRITER_CASES:
+            np.savez_compressed(os.path.join(wdir, "order.npz"), centers=c, radii=r, phases=p)
         c, r, p = sort_spheres(c, r, p)
         shots, miss, vox = parse_trace(log)
         vol = float(re.search(r"volume_of_spheres (\S+)", log).group(1))

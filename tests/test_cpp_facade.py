@@ -26,8 +26,12 @@ def test_facade_compiles_and_links():
 
 
 @pytest.mark.gpu
-def test_facade_runs_reference_scenario():
+def test_facade_runs_reference_scenario(tmp_path):
     exe = _compile()
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300, cwd=tmp_path)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "spheres" in r.stdout
+    vtp = tmp_path / "ParaviewOutput" / "rsa_mpi_0" / "rsa_mpi_0_0.vtp"
+    assert (tmp_path / "ParaviewOutput" / "rsa_mpi_0.pvtp").exists() and vtp.exists()
+    n = int(vtp.read_text().split('NumberOfPoints="')[1].split('"')[0])
+    assert 600 <= n <= 760
