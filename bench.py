@@ -105,7 +105,8 @@ class ClockSampler:
 
 
 FORM_NAMES = {0: "plain FP64", 1: "FP32 screen + FP64 guard-band retest"}
-FORM_KERNEL = {0: "k_refine_mask", 1: "k_refine_mask32"}
+# the mask pass: one kernel per launch (FP32 form: the cooperative kernel at level 0, the per-lane walk below)
+FORM_KERNEL = {0: "k_refine_mask", 1: "k_refine_mask32c (level 0) + k_refine_mask32"}
 
 
 def aggregate(times, counts, dist=None, device="cpu"):

@@ -25,6 +25,19 @@ constexpr int K_PRE = 12;  // prefilter spheres kept per parent voxel (more: re-
 // Child order of subdivide_uncovered: TabCorner (auxiliary/Path.ixx:86-103) for D = 2, 3; for D >= 4
 // bit d of the child index is the offset along dimension d (the reference's generic table,
 // Path.ixx:105-114, writes out of bounds and never sets dimension 0).
+// Corner-table position of the child with offset bit d = (j >> d) & 1: the inverse of child_bits.
+__device__ __forceinline__ int corner_of_child(int j) {
+    if (D == 2) {
+        const int tab = 0 | (3 << 2) | (2 << 4) | (1 << 6);
+        return (tab >> (2 * j)) & 3;
+    } else if (D == 3) {
+        const uint32_t tab = 0u | (7u << 3) | (4u << 6) | (3u << 9) | (2u << 12) | (5u << 15) | (6u << 18) | (1u << 21);
+        return (tab >> (3 * j)) & 7;
+    } else {
+        return j;
+    }
+}
+
 __device__ __forceinline__ int corner_bit(int t, int d) {
     if (D == 2) {
         const int tab = 0b01101100;  // (0,0) (1,1) (0,1) (1,0): bit (2t + d)
@@ -82,21 +95,65 @@ __host__ __device__ inline Geo<D> make_geo(const GridArgs& a) {
 inline unsigned nblocks(uint64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
 // ------------------------------------------------------------------------------------------------
-// level-0 voxel list, dimension 0 fastest (getAllIndices, auxiliary/Loops.ixx:45-69)
+// level-0 voxel list: the lattice of getAllIndices (auxiliary/Loops.ixx:45-69) in Morton order
+// (morton_select); the list order is free (the reference's own order only matters to its own darts)
 // ------------------------------------------------------------------------------------------------
 struct NVox {
     int64_t n[D];
 };
 
+// Entry v of the lattice n[0] x .. x n[D-1] in Morton (Z) order: the coordinates' bits interleaved level
+// by level, dimension D-1 most significant within a level, the points outside the box skipped.  Found by
+// descending the implicit 2^D-tree: at each bit, the points of the current prefix with that bit 0 are
+// counted as a box intersected with the lattice.  Children are written in Morton order next to their
+// parent at every refinement (k_refine_write), so the list stays in Morton order at every level and any
+// few consecutive entries, however sparse the list, lie close together in space: the cooperative mask
+// pass (k_refine_mask32c) relies on it.
+__device__ __forceinline__ void morton_select(uint64_t v, const int64_t* n, int64_t* out) {
+    int L = 0;
+#pragma unroll
+    for (int d = 0; d < D; d++)
+        while (L < 62 && (1ll << L) < n[d]) L++;
+    uint64_t f[D];
+    int nb[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        f[d] = 0;
+        nb[d] = 0;
+    }
+    for (int l = L - 1; l >= 0; l--) {
+#pragma unroll
+        for (int d = D - 1; d >= 0; d--) {
+            uint64_t cnt = 1;
+#pragma unroll
+            for (int e = 0; e < D; e++) {
+                uint64_t fe = f[e];
+                int free_bits = L - nb[e];
+                if (e == d) {
+                    fe *= 2;
+                    free_bits -= 1;
+                }
+                const int64_t lo = (int64_t)(fe << free_bits), hi = (int64_t)((fe + 1) << free_bits);
+                const int64_t c = (hi < n[e] ? hi : n[e]) - lo;
+                cnt *= c > 0 ? (uint64_t)c : 0;
+            }
+            if (v < cnt) {
+                f[d] = 2 * f[d];
+            } else {
+                v -= cnt;
+                f[d] = 2 * f[d] + 1;
+            }
+            nb[d]++;
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < D; d++) out[d] = (int64_t)f[d];
+}
+
 __global__ void k_vox_init(int64_t* vox, uint64_t V, NVox nv) {
     const uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
-    uint64_t r = v;
-#pragma unroll
-    for (int d = 0; d < D; d++) {
-        vox[v * D + d] = (int64_t)(r % (uint64_t)nv.n[d]);
-        r /= (uint64_t)nv.n[d];
-    }
+    morton_select(v, nv.n, vox + v * D);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -902,110 +959,190 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask(Grid<D> g, Geo<D> 
 // origin, centre and their offsets from the centre's cell corner are computed in FP64 (O(D) work);
 // each (voxel, sphere) test is FP32 unless it falls inside the guard band, where it is redone in FP64
 // exactly as the FP64 kernel does.
+// The voxel centre in cell edges, y = (cc + 1/2) len / c, in fixed point (fixed_cell): its integer part is the
+// cell k, its fraction the centre's offset relc from the cell's corner; relo is the voxel origin's offset.
+// Integer instructions only; the FP64 pipe of this GPU runs at 1/64 of the FP32 rate.  The error (below 2^-31
+// cell edges) is far inside the guard band, and only the screen uses these values.
+__device__ __forceinline__ void voxel_query32(const Grid<D>& g, const RefineParams& p, const int64_t* cc, int32_t* k,
+                                              float* relc, float* relo) {
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        int64_t kd;
+        uint32_t fb;
+        fixed_cell((uint64_t)cc[d], 1ull << 52, p.rho_int[d], p.rho_frac[d], p.level, kd, fb);
+        if (kd >= g.n[d]) kd -= g.n[d];  // the top face rounds onto the periodic image of cell 0
+        k[d] = (int32_t)(kd < g.n[d] ? kd : g.n[d] - 1);
+        relc[d] = __fmul_rn(__fmul_rn(__uint2float_rn(fb), 0x1p-32f), g.cf[d]);
+        relo[d] = __fsub_rn(relc[d], __fmul_rn(0.5f, p.lenf[d]));
+    }
+}
+
+// Exact FP64 quantities of the guard band for the voxel cc.  The empty volatile asm pins them inside the
+// guard-band branches: loop-invariant, they would otherwise be hoisted onto the common path, where FP64
+// instructions cost 64 FP32 ones on this GPU.
+struct Exact64 {
+    const Grid<D>& g;
+    const Geo<D>& geo;
+    const RefineParams& p;
+    const int64_t* cc;
+    // the voxel's origin and centre (list_of_voxels.ixx:154-160)
+    __device__ __forceinline__ void corners(double* orig, double* centre) const {
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            int64_t cv = cc[d];
+            asm volatile("" : "+l"(cv));
+            orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cv, p.len[d]));
+            centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cv, 0.5), p.len[d]));
+        }
+    }
+    // image of sphere idx (shift q) minus the voxel's origin and centre
+    __device__ __forceinline__ void deltas(int64_t idx, const int8_t* q, double* dl0, double* dl1) const {
+        double pp[D], img[D], orig[D], centre[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) pp[d] = g.pos[idx * D + d];
+        image_of<D>(geo, pp, q, img);
+        corners(orig, centre);
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            dl0[d] = __dsub_rn(img[d], orig[d]);
+            dl1[d] = __dsub_rn(img[d], centre[d]);
+        }
+    }
+    // bits of (r_s + r_min)^2
+    __device__ __forceinline__ uint64_t R2b(int64_t idx) const {
+        double rs = g.mono ? g.rmono : g.rad[idx];
+        asm volatile("" : "+d"(rs));
+        const double R = __dadd_rn(rs, p.rmin);
+        return dbits(__dmul_rn(R, R));
+    }
+};
+
+enum : int { PAIR_NONE = 0, PAIR_COVERS = 1, PAIR_PRE = 2 };
+
+// One (voxel, sphere) pair of the FP32 form: the sphere at cell offset o (offsets offs from its cell corner,
+// radius rs) against the voxel's centre and corners.  Returns PAIR_COVERS when the sphere holds every corner
+// (remove_covered, list_of_voxels.ixx:30-54), PAIR_PRE when it enters the prefilter list of the children
+// (get_list_of_spheres, :283-307), PAIR_NONE otherwise; d0, d1 receive the FP32 model deltas from the
+// voxel's origin and centre.  Decided in FP32 outside the guard band, in FP64 inside it (sphere idx, image
+// shift q), exactly as the FP64 kernel decides.
+template <class Locate>
+__device__ __forceinline__ int pair32(const Grid<D>& g, const RefineParams& p, const Exact64& ex, const int32_t* o,
+                                      const float* offs, float rs, const float* relc, const float* relo, float* d0,
+                                      float* d1, Locate&& locate, uint32_t& rt) {
+    const float R = __fadd_rn(rs, p.rminf);
+    const float R2 = __fmul_rn(R, R);
+    const float lo = __fsub_rn(R2, g.guard), hi = __fadd_rn(R2, g.guard);
+    model_delta<D>(g.cf, o, offs, relc, d1);
+    const float s1 = sumsq32<D>(d1);
+    if (s1 > hi) return PAIR_NONE;  // far: covers nothing, not in the prefilter list
+    model_delta<D>(g.cf, o, offs, relo, d0);
+    float m = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const float a = fmaxf(fabsf(d0[d]), fabsf(__fsub_rn(p.lenf[d], d0[d])));
+        m = __fadd_rn(m, __fmul_rn(a, a));
+    }
+    if (m < lo) return PAIR_COVERS;
+    bool in_pre = s1 < lo;
+    if (m <= hi || (!in_pre && s1 <= hi)) {
+        // guard band: redo this pair in FP64, as the FP64 kernel does
+        rt++;
+        int64_t idx;
+        int8_t q[D];
+        locate(idx, q);
+        double dl0[D], dl1[D];
+        ex.deltas(idx, q, dl0, dl1);
+        const uint64_t R2b = ex.R2b(idx);
+        double mm = 0.0, ss = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const double a = maxabs(dl0[d], __dsub_rn(p.len[d], dl0[d]));
+            const double sq = __dmul_rn(a, a);
+            mm = d == 0 ? sq : __dadd_rn(mm, sq);
+            const double s2 = __dmul_rn(dl1[d], dl1[d]);
+            ss = d == 0 ? s2 : __dadd_rn(ss, s2);
+        }
+        if (dbits(mm) <= R2b) return PAIR_COVERS;
+        in_pre = dbits(ss) < R2b;
+    }
+    return in_pre ? PAIR_PRE : PAIR_NONE;
+}
+
+// Children of one prefilter sphere (FP32 deltas d0, d1 from the parent's origin and centre, radius rs): the
+// bits of the children it covers.  Any child inside the guard band -> this sphere in FP64 (sphere idx,
+// image shift q), as children_covered.
+template <class Locate>
+__device__ __forceinline__ void children32(const Grid<D>& g, const RefineParams& p, const Exact64& ex,
+                                           const float* d0, const float* d1, float rs, Locate&& locate,
+                                           uint32_t* c32, uint32_t& rt) {
+    const float R = __fadd_rn(rs, p.rminf);
+    const float R2 = __fmul_rn(R, R);
+    const float lo = __fsub_rn(R2, g.guard), hi = __fadd_rn(R2, g.guard);
+    bool band = false;
+#pragma unroll
+    for (int w = 0; w < MASK_WORDS; w++) c32[w] = 0;
+    for (int t = 0; t < CHILDREN; t++) {
+        const int jb = child_bits(t);
+        float acc = 0.f;
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const float dd = ((jb >> d) & 1) ? d1[d] : d0[d];
+            const float a = fmaxf(fabsf(dd), fabsf(__fsub_rn(p.nlenf[d], dd)));
+            acc = __fadd_rn(acc, __fmul_rn(a, a));
+        }
+        if (acc < lo) c32[t >> 5] |= 1u << (t & 31);
+        else if (acc <= hi) band = true;
+    }
+    if (band) {
+        rt++;
+        int64_t idx;
+        int8_t q[D];
+        locate(idx, q);
+        double dl0[D], dl1[D];
+        ex.deltas(idx, q, dl0, dl1);
+        const uint64_t R2b = ex.R2b(idx);
+        if constexpr (CHILDREN <= 32) c32[0] = children_covered(dl0, dl1, p.nlen, R2b);
+        else {
+#pragma unroll
+            for (int w = 0; w < MASK_WORDS; w++) c32[w] = 0;
+            children_covered_wide(dl0, dl1, p.nlen, R2b, c32);
+        }
+    }
+}
+
 __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D>& geo, const RefineParams& p,
                                                    const int64_t* cc, uint32_t* mask, uint32_t& visits, uint32_t& rt) {
     bool survived = false;
     {
         float relo[D], relc[D];
         int32_t k[D];
-#pragma unroll
-        for (int d = 0; d < D; d++) {
-            // The voxel centre in cell edges, y = (cc + 1/2) len / c, in fixed point (fixed_cell): its integer
-            // part is the cell, its fraction the centre's offset from the cell's corner.  Integer instructions
-            // only; the FP64 pipe of this GPU runs at 1/64 of the FP32 rate.  The error (below 2^-31 cell edges)
-            // is far inside the guard band, and only the screen uses these values.
-            int64_t kd;
-            uint32_t fb;
-            fixed_cell((uint64_t)cc[d], 1ull << 52, p.rho_int[d], p.rho_frac[d], p.level, kd, fb);
-            if (kd >= g.n[d]) kd -= g.n[d];  // the top face rounds onto the periodic image of cell 0
-            k[d] = (int32_t)(kd < g.n[d] ? kd : g.n[d] - 1);
-            relc[d] = __fmul_rn(__fmul_rn(__uint2float_rn(fb), 0x1p-32f), g.cf[d]);
-            relo[d] = __fsub_rn(relc[d], __fmul_rn(0.5f, p.lenf[d]));
-        }
-        // the exact FP64 origin and centre (list_of_voxels.ixx:154-160), for the guard band only.  The empty
-        // volatile asm pins the computation inside the guard-band branch: loop-invariant, it would otherwise be
-        // hoisted onto the common path, where FP64 instructions cost 64 FP32 ones on this GPU.
-        auto exact_corners = [&](double* orig, double* centre) {
-#pragma unroll
-            for (int d = 0; d < D; d++) {
-                int64_t cv = cc[d];
-                asm volatile("" : "+l"(cv));
-                orig[d] = __dadd_rn(p.inf[d], __dmul_rn((double)cv, p.len[d]));
-                centre[d] = __dadd_rn(p.inf[d], __dmul_rn(__dadd_rn((double)cv, 0.5), p.len[d]));
-            }
-        };
-        float pre0[K_PRE][D], pre1[K_PRE][D], preR2[K_PRE];
+        voxel_query32(g, p, cc, k, relc, relo);
+        const Exact64 ex{g, geo, p, cc};
+        float pre0[K_PRE][D], pre1[K_PRE][D], prers[K_PRE];
         int64_t preidx[K_PRE];
         uint32_t preq[K_PRE];  // 2 bits per dimension: image shift + 1
         int npre = 0;
         bool overflow = false;
-        // exact FP64 differences of one (voxel, sphere) pair, for the guard band
-        auto exact_deltas = [&](int64_t idx, const int8_t* q, double* dl0, double* dl1) {
-            double pp[D], img[D], orig[D], centre[D];
-#pragma unroll
-            for (int d = 0; d < D; d++) pp[d] = g.pos[idx * D + d];
-            image_of<D>(geo, pp, q, img);
-            exact_corners(orig, centre);
-#pragma unroll
-            for (int d = 0; d < D; d++) {
-                dl0[d] = __dsub_rn(img[d], orig[d]);
-                dl1[d] = __dsub_rn(img[d], centre[d]);
-            }
-        };
-        auto exact_R2b = [&](int64_t idx) {
-            double rs = g.mono ? g.rmono : g.rad[idx];
-            asm volatile("" : "+d"(rs));  // kept in the guard-band branch (see exact_corners)
-            const double R = __dadd_rn(rs, p.rmin);
-            return dbits(__dmul_rn(R, R));
-        };
         const float R2q = search_r2(p.rmin, g.rmax);
         const bool covered = visit_placed_o<D>(g, k, relc, R2q, [&](int64_t idx, const int32_t* o, const int8_t* q) {
             visits++;
             const float rs = g.mono ? g.rmonof : g.radf[idx];
-            const float R = __fadd_rn(rs, p.rminf);
-            const float R2 = __fmul_rn(R, R);
-            const float lo = __fsub_rn(R2, g.guard), hi = __fadd_rn(R2, g.guard);
-            const float* offs = g.off + idx * D;
-            float d1[D];
-            model_delta<D>(g.cf, o, offs, relc, d1);
-            const float s1 = sumsq32<D>(d1);
-            if (s1 > hi) return false;  // far: covers nothing, not in the prefilter list
-            float d0[D];
-            model_delta<D>(g.cf, o, offs, relo, d0);
-            float m = 0.f;
+            float d0[D], d1[D];
+            const int r = pair32(g, p, ex, o, g.off + idx * D, rs, relc, relo, d0, d1,
+                                 [&](int64_t& i2, int8_t* q2) {
+                                     i2 = idx;
 #pragma unroll
-            for (int d = 0; d < D; d++) {
-                const float a = fmaxf(fabsf(d0[d]), fabsf(__fsub_rn(p.lenf[d], d0[d])));
-                m = __fadd_rn(m, __fmul_rn(a, a));
-            }
-            if (m < lo) return true;  // the parent is covered
-            bool in_pre = s1 < lo;
-            if (m <= hi || (!in_pre && s1 <= hi)) {
-                // guard band: redo this pair in FP64, as the FP64 kernel does
-                rt++;
-                double dl0[D], dl1[D];
-                exact_deltas(idx, q, dl0, dl1);
-                const uint64_t R2b = exact_R2b(idx);
-                double mm = 0.0, ss = 0.0;
-#pragma unroll
-                for (int d = 0; d < D; d++) {
-                    const double a = maxabs(dl0[d], __dsub_rn(p.len[d], dl0[d]));
-                    const double sq = __dmul_rn(a, a);
-                    mm = d == 0 ? sq : __dadd_rn(mm, sq);
-                    const double s2 = __dmul_rn(dl1[d], dl1[d]);
-                    ss = d == 0 ? s2 : __dadd_rn(ss, s2);
-                }
-                if (dbits(mm) <= R2b) return true;
-                in_pre = dbits(ss) < R2b;
-            }
-            if (in_pre) {
+                                     for (int d = 0; d < D; d++) q2[d] = q[d];
+                                 }, rt);
+            if (r == PAIR_COVERS) return true;  // the parent is covered
+            if (r == PAIR_PRE) {
                 if (npre < K_PRE) {
 #pragma unroll
                     for (int d = 0; d < D; d++) {
                         pre0[npre][d] = d0[d];
                         pre1[npre][d] = d1[d];
                     }
-                    preR2[npre] = R2;
+                    prers[npre] = rs;
                     preidx[npre] = idx;
                     uint32_t qq = 0;
 #pragma unroll
@@ -1025,38 +1162,16 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
             for (int w = 0; w < MASK_WORDS; w++) cov[w] = 0;
             for (int sidx = 0; sidx < npre; sidx++) {
                 // children of this sphere in FP32; any child inside the guard band -> this sphere in FP64
-                const float lo = __fsub_rn(preR2[sidx], g.guard), hi = __fadd_rn(preR2[sidx], g.guard);
-                bool band = false;
+                int8_t q[D];
+#pragma unroll
+                for (int d = 0; d < D; d++) q[d] = (int8_t)((preq[sidx] >> (2 * d)) & 3u) - 1;
                 uint32_t c32[MASK_WORDS];
+                children32(g, p, ex, pre0[sidx], pre1[sidx], prers[sidx],
+                           [&](int64_t& i2, int8_t* q2) {
+                               i2 = preidx[sidx];
 #pragma unroll
-                for (int w = 0; w < MASK_WORDS; w++) c32[w] = 0;
-                for (int t = 0; t < CHILDREN; t++) {
-                    const int jb = child_bits(t);
-                    float acc = 0.f;
-#pragma unroll
-                    for (int d = 0; d < D; d++) {
-                        const float dd = ((jb >> d) & 1) ? pre1[sidx][d] : pre0[sidx][d];
-                        const float a = fmaxf(fabsf(dd), fabsf(__fsub_rn(p.nlenf[d], dd)));
-                        acc = __fadd_rn(acc, __fmul_rn(a, a));
-                    }
-                    if (acc < lo) c32[t >> 5] |= 1u << (t & 31);
-                    else if (acc <= hi) band = true;
-                }
-                if (band) {
-                    rt++;
-                    int8_t q[D];
-#pragma unroll
-                    for (int d = 0; d < D; d++) q[d] = (int8_t)((preq[sidx] >> (2 * d)) & 3u) - 1;
-                    double dl0[D], dl1[D];
-                    exact_deltas(preidx[sidx], q, dl0, dl1);
-                    const uint64_t R2b = exact_R2b(preidx[sidx]);
-                    if constexpr (CHILDREN <= 32) c32[0] = children_covered(dl0, dl1, p.nlen, R2b);
-                    else {
-#pragma unroll
-                        for (int w = 0; w < MASK_WORDS; w++) c32[w] = 0;
-                        children_covered_wide(dl0, dl1, p.nlen, R2b, c32);
-                    }
-                }
+                               for (int d = 0; d < D; d++) q2[d] = q[d];
+                           }, c32, rt);
 #pragma unroll
                 for (int w = 0; w < MASK_WORDS; w++) cov[w] |= c32[w];
             }
@@ -1066,7 +1181,7 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
 #pragma unroll
                 for (int w = 0; w < MASK_WORDS; w++) cov[w] = 0;
                 double orig[D], centre[D];
-                exact_corners(orig, centre);
+                ex.corners(orig, centre);
                 visit_placed<D>(g, geo, k, relc, R2q, [&](int64_t idx, const double* img, double rs) {
                     const double R = __dadd_rn(rs, p.rmin);
                     const uint64_t R2b = dbits(__dmul_rn(R, R));
@@ -1131,6 +1246,303 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask32(Grid<D> g, Geo<D
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// Cooperative FP32 mask pass.  Groups of COOP_G consecutive voxels of the list (siblings, or neighbours in
+// the Morton order of the list) gather the occupied cells around their common box of cells once, into
+// shared memory, and every lane tests its own voxel against that list in step with the others: no per-lane
+// stencil walk with its divergent row loops.  A group whose voxels lie too far apart (union wider than one
+// occupancy window, more rows than COOP_ROWS_MAX or more than COOP_CAND spheres) takes the per-lane walk
+// (refine_mask32_body).  The decisions are those of k_refine_mask32: the group's list holds every sphere
+// within reach of each of its voxels' centres, the per-pair tests are the same functions (pair32,
+// children32), and the results (covered, prefilter set, child masks) do not depend on the visiting order.
+// ------------------------------------------------------------------------------------------------
+constexpr int COOP_G = 8;
+constexpr int COOP_CAND = 64;
+constexpr int COOP_BLOCK = 128;
+constexpr int COOP_ROWS_MAX = 1024;
+
+// Padding (in 4-byte words) that brings a list of `words` words to `target` modulo 32 banks.
+constexpr int list_pad(int words, int target) {
+    return ((target - words % 32) % 32 + 32) % 32 == 0 ? 32 : ((target - words % 32) % 32 + 32) % 32;
+}
+
+// A group's sphere list in shared memory.  The groups of a warp read the same slot of their own lists in
+// step: the padding puts consecutive lists BANK_STEP banks apart, free of bank conflicts.
+template <int CAND, int BANK_STEP>
+struct SphereList {
+    float off[D][CAND];  // the sphere's offsets from its cell corner
+    float rs[CAND];      // its radius
+    int16_t t[D][CAND];  // its image's cell: base + t (unwrapped)
+    float pad[list_pad(D * CAND + CAND + D * CAND / 2, BANK_STEP)];
+};
+using CoopList = SphereList<COOP_CAND, 8>;  // four 8-lane groups per warp
+static_assert((sizeof(CoopList) / 4) % 32 == 8, "CoopList bank spacing");
+
+// Row t[1..D-1] of the group's union: the wrapped linear base of its cells (times n_0) and the dimension-0
+// range [t0lo, t0hi] within reach of the box [kmin, kmax] of the group's cells (false: the row is out of
+// reach).  sqrt.approx and the reciprocal cell edge stand for the exact operations: the search radius
+// carries a 1e-4 margin, far above their error.
+__device__ __forceinline__ bool coop_row(const Grid<D>& g, const int32_t* t, const int32_t* kb, const int32_t* kmin,
+                                         const int32_t* kmax, const int32_t* w, float R2q, int64_t& base,
+                                         int32_t& t0lo, int32_t& t0hi) {
+    float rest = 0.f;
+#pragma unroll
+    for (int d = 1; d < D; d++) {
+        const int32_t u = kb[d] + t[d];
+        const int32_t gap = u < kmin[d] ? kmin[d] - u - 1 : (u > kmax[d] ? u - kmax[d] - 1 : 0);
+        const float gf = __fmul_rn((float)gap, g.cf[d]);
+        rest = __fadd_rn(rest, __fmul_rn(gf, gf));
+    }
+    if (rest > R2q) return false;
+    base = 0;
+#pragma unroll
+    for (int d = D - 1; d >= 1; d--) {
+        int32_t kk = kb[d] + t[d];
+        kk = kk < 0 ? kk + g.n[d] : (kk >= g.n[d] ? kk - g.n[d] : kk);
+        base = base * g.n[d] + kk;
+    }
+    base *= g.n[0];
+    const int32_t mx = 1 + __float2int_rd(__fmul_rn(sqrt_approx(__fsub_rn(R2q, rest)), g.inv_c0f));
+    const int32_t m0 = kmin[0] - kb[0];
+    t0lo = max(0, m0 - mx);
+    t0hi = min(w[0] - 1, m0 + (kmax[0] - kmin[0]) + mx);
+    return t0lo <= t0hi;
+}
+
+// Occupancy bits of cells t0lo..t0hi of a row (at most 32 cells, wrapped along dimension 0 in up to two
+// pieces): bit i = cell t0lo + i.
+__device__ __forceinline__ uint32_t coop_row_bits(const Grid<D>& g, int64_t base, int32_t kb0, int32_t t0lo,
+                                                  int32_t t0hi) {
+    const int32_t n0 = g.n[0];
+    uint32_t bits = 0;
+    int32_t t = t0lo;
+    while (t <= t0hi) {
+        const int32_t u = kb0 + t;
+        const int32_t x = u < 0 ? u + n0 : (u >= n0 ? u - n0 : u);
+        // cells of this piece: up to the wrap point or the end of the range
+        const int32_t piece_end = u < 0 ? min(t0hi, -1 - kb0) : (u >= n0 ? t0hi : min(t0hi, n0 - 1 - kb0));
+        const int32_t len = piece_end - t + 1;
+        bits |= occ_bits(g.occ, base + x, len) << (t - t0lo);
+        t += len;
+    }
+    return bits;
+}
+
+// The voxel cc (cell k, offsets relc / relo) against a group's list (slots 0..total-1, cells base + t):
+// remove_covered over the list, then the children of the prefilter spheres, as refine_mask32_body does
+// over its walk.  Fills mask; returns true when the voxel survives.
+template <class List>
+__device__ __forceinline__ bool list_test(const Grid<D>& g, const Geo<D>& geo, const RefineParams& p, const List& L,
+                                          uint32_t total, const int32_t* base, const int32_t* k, const float* relc,
+                                          const float* relo, const int64_t* cc, uint32_t* mask, uint32_t& rt) {
+    const Exact64 ex{g, geo, p, cc};
+    // the sphere of slot j: linear index and image shift, for the guard band only
+    auto sphere_of = [&](uint32_t j, int64_t& idx, int8_t* q) {
+        idx = 0;
+#pragma unroll
+        for (int d = D - 1; d >= 0; d--) {
+            const int32_t u = base[d] + (int32_t)L.t[d][j];
+            q[d] = u < 0 ? -1 : (u >= g.n[d] ? 1 : 0);
+            idx = idx * g.n[d] + (u - (int32_t)q[d] * g.n[d]);
+        }
+    };
+    int32_t ob[D];  // cell offset of slot t = 0 from this voxel's cell
+#pragma unroll
+    for (int d = 0; d < D; d++) ob[d] = base[d] - k[d];
+    uint64_t pre = 0;
+    for (uint32_t j = 0; j < total; j++) {
+        int32_t o[D];
+        float offs[D], d0[D], d1[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            o[d] = ob[d] + (int32_t)L.t[d][j];
+            offs[d] = L.off[d][j];
+        }
+        const int r = pair32(g, p, ex, o, offs, L.rs[j], relc, relo, d0, d1,
+                             [&](int64_t& idx, int8_t* q) { sphere_of(j, idx, q); }, rt);
+        if (r == PAIR_COVERS) return false;
+        if (r == PAIR_PRE) pre |= 1ull << j;
+    }
+    uint32_t cov[MASK_WORDS];
+#pragma unroll
+    for (int w2 = 0; w2 < MASK_WORDS; w2++) cov[w2] = 0;
+    while (pre) {
+        const uint32_t j = (uint32_t)(__ffsll((long long)pre) - 1);
+        pre &= pre - 1;
+        int32_t o[D];
+        float offs[D], d0[D], d1[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            o[d] = ob[d] + (int32_t)L.t[d][j];
+            offs[d] = L.off[d][j];
+        }
+        model_delta<D>(g.cf, o, offs, relc, d1);
+        model_delta<D>(g.cf, o, offs, relo, d0);
+        uint32_t c32[MASK_WORDS];
+        children32(g, p, ex, d0, d1, L.rs[j], [&](int64_t& idx, int8_t* q) { sphere_of(j, idx, q); }, c32, rt);
+#pragma unroll
+        for (int w2 = 0; w2 < MASK_WORDS; w2++) cov[w2] |= c32[w2];
+    }
+#pragma unroll
+    for (int w2 = 0; w2 < MASK_WORDS; w2++) {
+        const int bits_here = CHILDREN - 32 * w2 < 32 ? CHILDREN - 32 * w2 : 32;
+        const uint32_t all = bits_here >= 32 ? 0xffffffffu : ((1u << bits_here) - 1u);
+        mask[w2] = ~cov[w2] & all;
+    }
+    return true;
+}
+
+// Writes the voxel's child mask and the warp's child count, survivors, visits and retests (all lanes).
+__device__ __forceinline__ void mask_epilogue(const RefineParams& p, uint64_t v, bool active, const uint32_t* mask,
+                                              bool survived, uint32_t visits, uint32_t rt) {
+    if (active) {
+#pragma unroll
+        for (int w2 = 0; w2 < MASK_WORDS; w2++) p.masks[v * MASK_WORDS + w2] = mask[w2];
+    }
+    uint32_t cntc = 0;
+#pragma unroll
+    for (int w2 = 0; w2 < MASK_WORDS; w2++) cntc += __popc(mask[w2]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cntc += __shfl_xor_sync(0xffffffffu, cntc, o);
+    const uint32_t alive = __ballot_sync(0xffffffffu, survived);
+    uint32_t wv = visits, wr = rt;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        wv += __shfl_xor_sync(0xffffffffu, wv, o);
+        wr += __shfl_xor_sync(0xffffffffu, wr, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        const uint64_t warp = v >> 5;
+        if (warp * 32 < p.V) p.warp_counts[warp] = cntc;
+        if (alive) atomicAdd(p.survivors, (uint32_t)__popc(alive));
+        if (wv) atomicAdd(p.visits, (unsigned long long)wv);
+        if (wr) atomicAdd(p.retests, (unsigned long long)wr);
+    }
+}
+
+__global__ void __launch_bounds__(COOP_BLOCK) k_refine_mask32c(Grid<D> g, Geo<D> geo, RefineParams p) {
+    __shared__ CoopList lists[COOP_BLOCK / COOP_G];
+    const uint64_t v = (uint64_t)blockIdx.x * COOP_BLOCK + threadIdx.x;
+    const int gl = threadIdx.x & (COOP_G - 1);
+    CoopList& L = lists[threadIdx.x / COOP_G];
+    const bool active = v < p.V;
+    int64_t cc[D];
+    int32_t k[D];
+    float relc[D], relo[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        cc[d] = active ? p.vin[v * D + d] : 0;
+        k[d] = 0;
+        relc[d] = relo[d] = 0.f;
+    }
+    if (active) voxel_query32(g, p, cc, k, relc, relo);
+    // the group's box of cells and its union of reach
+    const float R2q = search_r2(p.rmin, g.rmax);
+    const float sq = __fsqrt_rn(R2q);
+    int32_t kmin[D], kmax[D], kb[D], w[D];
+    bool ok = true;
+    int64_t rows = 1;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        int32_t lo = active ? k[d] : 0x7fffffff, hi = active ? k[d] : -1;
+#pragma unroll
+        for (int o = 1; o < COOP_G; o <<= 1) {
+            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        kmin[d] = lo;
+        kmax[d] = hi;
+        const int32_t m = 1 + (int32_t)floorf(__fdiv_rn(sq, g.cf[d]));
+        ok = ok && hi >= 0 && (int64_t)(hi - lo) + 1 + 2 * (int64_t)m <= (int64_t)g.n[d];
+        w[d] = ok ? hi - lo + 1 + 2 * m : 1;
+        kb[d] = lo - m;
+        if (d >= 1 && rows <= COOP_ROWS_MAX) rows *= w[d];  // saturates above the limit
+    }
+    ok = ok && w[0] <= 32 && rows <= COOP_ROWS_MAX;
+    // One pass over the union's rows, COOP_G rows per step (lane gl takes row step * COOP_G + gl, its
+    // coordinates t[1..D-1] advanced by COOP_G in mixed radix w, dimension 1 fastest): occupied cells ->
+    // the group's list, in row order, slots from a scan within the group.  Past COOP_CAND the group only
+    // counts, and falls back to the per-lane walk.
+    const uint32_t gmask = 0xffu << (threadIdx.x & 31 & ~(COOP_G - 1));
+    uint32_t total = 0;
+    if (ok) {
+        int32_t t[D];
+        t[0] = 0;
+        {
+            int32_t r = gl;
+#pragma unroll
+            for (int d = 1; d < D; d++) {
+                int32_t q = 0;
+                while (r >= w[d]) {
+                    r -= w[d];
+                    q++;
+                }
+                t[d] = r;
+                r = q;
+            }
+        }
+        const int steps = ((int)rows + COOP_G - 1) / COOP_G;
+        for (int st = 0; st < steps; st++) {
+            const bool has_row = st * COOP_G + gl < (int)rows;
+            int64_t base = 0;
+            int32_t t0lo = 0, t0hi = -1;
+            uint32_t bits = 0;
+            if (has_row && coop_row(g, t, kb, kmin, kmax, w, R2q, base, t0lo, t0hi))
+                bits = coop_row_bits(g, base, kb[0], t0lo, t0hi);
+            const uint32_t c = __popc(bits);
+            uint32_t incl = c;
+#pragma unroll
+            for (int o = 1; o < COOP_G; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(gmask, incl, o, COOP_G);
+                if (gl >= o) incl += y;
+            }
+            uint32_t slot = total + incl - c;
+            total += __shfl_sync(gmask, incl, COOP_G - 1, COOP_G);
+            while (bits) {
+                const int j = __ffs(bits) - 1;
+                bits &= bits - 1;
+                if (slot < COOP_CAND) {
+                    const int32_t t0 = t0lo + j;
+                    const int32_t u = kb[0] + t0;
+                    const int64_t idx = base + (u < 0 ? u + g.n[0] : (u >= g.n[0] ? u - g.n[0] : u));
+#pragma unroll
+                    for (int d = 0; d < D; d++) L.off[d][slot] = g.off[idx * D + d];
+                    L.rs[slot] = g.mono ? g.rmonof : g.radf[idx];
+                    L.t[0][slot] = (int16_t)t0;
+#pragma unroll
+                    for (int d = 1; d < D; d++) L.t[d][slot] = (int16_t)t[d];
+                }
+                slot++;
+            }
+            // next row of this lane: t[1..] + COOP_G in mixed radix
+            if (D > 1) {
+                t[1] += COOP_G;
+#pragma unroll
+                for (int d = 1; d < D - 1; d++) {
+                    while (t[d] >= w[d]) {
+                        t[d] -= w[d];
+                        t[d + 1]++;
+                    }
+                }
+            }
+        }
+    }
+    ok = ok && total <= COOP_CAND;
+    __syncwarp();
+    uint32_t mask[MASK_WORDS];
+#pragma unroll
+    for (int w2 = 0; w2 < MASK_WORDS; w2++) mask[w2] = 0;
+    bool survived = false;
+    uint32_t visits = 0, rt = 0;
+    if (ok && active) {
+        if (gl == 0) visits = total;
+        survived = list_test(g, geo, p, L, total, kb, k, relc, relo, cc, mask, rt);
+    } else if (active) {
+        survived = refine_mask32_body(g, geo, p, cc, mask, visits, rt);
+    }
+    mask_epilogue(p, v, active, mask, survived, visits, rt);
+}
+
 __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
     const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
     uint32_t mask[MASK_WORDS];
@@ -1156,10 +1568,12 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
     int64_t cc[D];
 #pragma unroll
     for (int d = 0; d < D; d++) cc[d] = p.vin[v * D + d];
-    for (int t = 0; t < CHILDREN; t++) {
+    // children in Morton order (bit d of j = offset along d), which keeps the list in Morton order
+    for (int j = 0; j < CHILDREN; j++) {
+        const int t = corner_of_child(j);
         if (!((mask[t >> 5] >> (t & 31)) & 1u)) continue;
 #pragma unroll
-        for (int d = 0; d < D; d++) p.vout[o * D + d] = 2 * cc[d] + corner_bit(t, d);
+        for (int d = 0; d < D; d++) p.vout[o * D + d] = 2 * cc[d] + ((j >> d) & 1);
         o++;
     }
 }
@@ -1428,8 +1842,15 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
 
 void op_refine_mask(const GridArgs& ga, const RefineArgs& a, int f32, cudaStream_t s) {
     if (a.V == 0) return;
-    if (f32)
+    // Level 0 (one voxel per cell, neighbours in Morton order): 8-lane groups over their box of cells.  Deeper
+    // levels: the per-lane walk.  There the siblings share one cell and walk the same rows in step, and most
+    // voxels are covered by a sphere of the first rows, where the walk stops; measured on the 3D r = 0.002
+    // workload, a shared gather per cell (or a near-rows pass with the rest compacted) was slower.
+    if (f32 && a.level == 0) {
+        k_refine_mask32c<<<nblocks(a.V, COOP_BLOCK), COOP_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
+    } else if (f32) {
         k_refine_mask32<<<nblocks(a.V, REFINE_BLOCK), REFINE_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
+    }
     else
         k_refine_mask<<<nblocks(a.V, REFINE_BLOCK), REFINE_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
     count_launch();

@@ -33,19 +33,16 @@ __device__ __forceinline__ CandArgs with_lists(const CandArgs& c, const BInst& I
     return ci;
 }
 
-// level-0 voxels of every instance, dimension 0 fastest within each segment (as k_vox_init)
+// level-0 voxels of every instance, in Morton order within each segment (as k_vox_init)
 __global__ void k_b_vox_init(BatchArgs b, int64_t* vox) {
     const uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= b.V) return;
     const BInst* tab = (const BInst*)b.table;
     const uint32_t s = segment_of(b.vox_off, b.M, v);
-    uint64_t r = v - b.vox_off[s];
+    int64_t n[D];
 #pragma unroll
-    for (int d = 0; d < D; d++) {
-        const uint64_t n = (uint64_t)tab[s].nvox0[d];
-        vox[v * D + d] = (int64_t)(r % n);
-        r /= n;
-    }
+    for (int d = 0; d < D; d++) n[d] = tab[s].nvox0[d];
+    morton_select(v - b.vox_off[s], n, vox + v * D);
 }
 
 // Slot t of the round holds global dart g = perm[t] (or t): dart (g - dart_off[s]) of instance s, under the
@@ -348,10 +345,11 @@ __global__ void __launch_bounds__(256) k_b_refine_write(BatchArgs b, RefineArgs 
         for (int d = 0; d < D; d++) a.vout[o * D + d] = cc[d];
         return;
     }
-    for (int t = 0; t < CHILDREN; t++) {
+    for (int j = 0; j < CHILDREN; j++) {  // Morton order, as k_refine_write
+        const int t = corner_of_child(j);
         if (!((mask[t >> 5] >> (t & 31)) & 1u)) continue;
 #pragma unroll
-        for (int d = 0; d < D; d++) a.vout[o * D + d] = 2 * cc[d] + corner_bit(t, d);
+        for (int d = 0; d < D; d++) a.vout[o * D + d] = 2 * cc[d] + ((j >> d) & 1);
         o++;
     }
 }
