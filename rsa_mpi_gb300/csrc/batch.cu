@@ -126,6 +126,7 @@ struct Wave {
         dfree(c.next);
         dfree(c.alive);
         dfree(c.off);
+        dfree(c.radf);
         dfree(c.kc);
         dfree(c.blk);
         dfree(c.nblk);
@@ -155,6 +156,7 @@ void ensure_cand(Wave& W, int D, bool f32, uint64_t n) {
     W.c.alive = dalloc<uint32_t>(cap);
     if (f32) {
         W.c.off = dalloc<float>(cap * D);
+        W.c.radf = dalloc<float>(cap);
         W.c.kc = dalloc<int32_t>(cap * D);
     }
     W.c.blk = dalloc<int32_t>(cap * NB);

@@ -80,6 +80,7 @@ __host__ __device__ inline Grid<D> make_grid(const GridArgs& a) {
     g.mono = a.mono;
     g.rmono = a.rmono;
     g.rmonof = (float)a.rmono;
+    g.rmaxf = (float)a.rmax;
     return g;
 }
 
@@ -262,7 +263,7 @@ __device__ __forceinline__ void dart32_body(const DartParams& p, uint32_t i, uin
         if (kd >= p.ncell[d]) kd -= p.ncell[d];
         kd = kd < p.ncell[d] ? kd : p.ncell[d] - 1;
         p.kc[o * D + d] = (int32_t)kd;
-        p.off[o * D + d] = __fmul_rn(__fmul_rn(__uint2float_rn(fr), 0x1p-32f), p.cf[d]);
+        p.off[o * D + d] = __fmul_rn(__fmul_rn(u32_to_float(fr), 0x1p-32f), p.cf[d]);
     }
     p.key[o] = ((uint64_t)w[2 + 2 * D] << 32) | i;
     p.rad[o] = dart_radius(p, i);
@@ -380,8 +381,9 @@ __device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, 
             k[d] = c.kc[(uint64_t)i * D + d];
             offq[d] = c.off[(uint64_t)i * D + d];
         }
-        const float rf = __double2float_rn(r);
-        hit = visit_placed_o<D>(g, k, offq, search_r2(r, g.rmax), [&](int64_t idx, const int32_t* o, const int8_t* q) {
+        float rf = __double2float_rn(r);
+        asm volatile("" : "+f"(rf));  // not rematerialised in the loop below: the conversion runs on the FP64 pipe
+        hit = visit_placed_o<D>(g, k, offq, search_r2f(rf, g.rmaxf), [&](int64_t idx, const int32_t* o, const int8_t* q) {
             const float rs = g.mono ? g.rmonof : g.radf[idx];
             const float R = __fadd_rn(rf, rs);
             const float R2 = __fmul_rn(R, R);
@@ -413,6 +415,7 @@ __device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, 
         c.state[i] = ST_DEAD;
         return false;
     }
+    if (F32) c.radf[i] = __double2float_rn(r);
     const int64_t idx = cell_index<D>(g, k);
     c.cell[i] = idx;
     c.next[i] = atomicExch(c.head + idx, (int32_t)i);
@@ -487,7 +490,7 @@ __device__ __forceinline__ void visit_candidates_o(const Grid<D>& g, const CandA
 __device__ __forceinline__ bool cand_collide32(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, const double* x,
                                                double r, const float* offq, float rf, int32_t j, const int32_t* o,
                                                const int8_t* q, uint32_t& rt) {
-    const float R = __fadd_rn(rf, __double2float_rn(c.rad[j]));
+    const float R = __fadd_rn(rf, c.radf[j]);
     const float R2 = __fmul_rn(R, R);
     float dlt[D];
     model_delta<D>(g.cf, o, c.off + (uint64_t)j * D, offq, dlt);
@@ -552,8 +555,9 @@ __device__ __forceinline__ bool collect_body(const Grid<D>& g, const Geo<D>& geo
                 k[d] = c.kc[(uint64_t)i * D + d];
                 offq[d] = c.off[(uint64_t)i * D + d];
             }
-            const float rf = __double2float_rn(r);
-            visit_candidates_o(g, c, k, offq, search_r2(r, g.rmax), [&](int32_t j, const int32_t* o, const int8_t* q) {
+            float rf = __double2float_rn(r);
+        asm volatile("" : "+f"(rf));  // not rematerialised in the loop below: the conversion runs on the FP64 pipe
+            visit_candidates_o(g, c, k, offq, search_r2f(rf, g.rmaxf), [&](int32_t j, const int32_t* o, const int8_t* q) {
                 if (!precedes(c.key[j], j, key, i)) return false;
                 if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) record(j);
                 return false;
@@ -622,8 +626,9 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
                             k[d] = c.kc[(uint64_t)i * D + d];
                             offq[d] = c.off[(uint64_t)i * D + d];
                         }
-                        const float rf = __double2float_rn(r);
-                        visit_candidates_o(g, c, k, offq, search_r2(r, g.rmax), [&](int32_t j, const int32_t* o, const int8_t* q) {
+                        float rf = __double2float_rn(r);
+        asm volatile("" : "+f"(rf));  // not rematerialised in the loop below: the conversion runs on the FP64 pipe
+                        visit_candidates_o(g, c, k, offq, search_r2f(rf, g.rmaxf), [&](int32_t j, const int32_t* o, const int8_t* q) {
                             if (!precedes(c.key[j], j, key, i)) return false;
                             if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) judge(j);
                             return any_acc;
@@ -838,7 +843,7 @@ __device__ __forceinline__ bool refine_mask64_body(const Grid<D>& g, const Geo<D
         uint64_t preR2[K_PRE];
         int npre = 0;
         bool overflow = false;
-        const float R2q = search_r2(p.rmin, g.rmax);
+        const float R2q = search_r2f(p.rminf, g.rmaxf);
         const bool covered = visit_placed<D>(g, geo, k, qo, R2q, [&](int64_t, const double* img, double rs) {
             visits++;
             const double R = __dadd_rn(rs, p.rmin);
@@ -972,7 +977,7 @@ __device__ __forceinline__ void voxel_query32(const Grid<D>& g, const RefinePara
         fixed_cell((uint64_t)cc[d], 1ull << 52, p.rho_int[d], p.rho_frac[d], p.level, kd, fb);
         if (kd >= g.n[d]) kd -= g.n[d];  // the top face rounds onto the periodic image of cell 0
         k[d] = (int32_t)(kd < g.n[d] ? kd : g.n[d] - 1);
-        relc[d] = __fmul_rn(__fmul_rn(__uint2float_rn(fb), 0x1p-32f), g.cf[d]);
+        relc[d] = __fmul_rn(__fmul_rn(u32_to_float(fb), 0x1p-32f), g.cf[d]);
         relo[d] = __fsub_rn(relc[d], __fmul_rn(0.5f, p.lenf[d]));
     }
 }
@@ -1123,7 +1128,7 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
         uint32_t preq[K_PRE];  // 2 bits per dimension: image shift + 1
         int npre = 0;
         bool overflow = false;
-        const float R2q = search_r2(p.rmin, g.rmax);
+        const float R2q = search_r2f(p.rminf, g.rmaxf);
         const bool covered = visit_placed_o<D>(g, k, relc, R2q, [&](int64_t idx, const int32_t* o, const int8_t* q) {
             visits++;
             const float rs = g.mono ? g.rmonof : g.radf[idx];
@@ -1290,7 +1295,7 @@ __device__ __forceinline__ bool coop_row(const Grid<D>& g, const int32_t* t, con
     for (int d = 1; d < D; d++) {
         const int32_t u = kb[d] + t[d];
         const int32_t gap = u < kmin[d] ? kmin[d] - u - 1 : (u > kmax[d] ? u - kmax[d] - 1 : 0);
-        const float gf = __fmul_rn((float)gap, g.cf[d]);
+        const float gf = __fmul_rn(small_i2f(gap), g.cf[d]);
         rest = __fadd_rn(rest, __fmul_rn(gf, gf));
     }
     if (rest > R2q) return false;
@@ -1302,7 +1307,7 @@ __device__ __forceinline__ bool coop_row(const Grid<D>& g, const int32_t* t, con
         base = base * g.n[d] + kk;
     }
     base *= g.n[0];
-    const int32_t mx = 1 + __float2int_rd(__fmul_rn(sqrt_approx(__fsub_rn(R2q, rest)), g.inv_c0f));
+    const int32_t mx = 1 + small_floor(__fmul_rn(sqrt_approx(__fsub_rn(R2q, rest)), g.inv_c0f));
     const int32_t m0 = kmin[0] - kb[0];
     t0lo = max(0, m0 - mx);
     t0hi = min(w[0] - 1, m0 + (kmax[0] - kmin[0]) + mx);
@@ -1437,7 +1442,7 @@ __global__ void __launch_bounds__(COOP_BLOCK) k_refine_mask32c(Grid<D> g, Geo<D>
     }
     if (active) voxel_query32(g, p, cc, k, relc, relo);
     // the group's box of cells and its union of reach
-    const float R2q = search_r2(p.rmin, g.rmax);
+    const float R2q = search_r2f(p.rminf, g.rmaxf);
     const float sq = __fsqrt_rn(R2q);
     int32_t kmin[D], kmax[D], kb[D], w[D];
     bool ok = true;

@@ -57,6 +57,7 @@ struct Grid {
     float c0f;             // cell edge along dimension 0
     float inv_c0f;         // its inverse
     double rmax;           // largest radius the grid holds
+    float rmaxf;           // the same, rounded to float (search radii carry a margin far above that rounding)
     // FP32 screening representation of the placed centres (guard-band form): off = centre minus the
     // corner of its cell, rounded to float; radf = radius rounded to float
     const float* off;
@@ -184,6 +185,21 @@ __device__ __forceinline__ uint32_t occ_bits(const uint32_t* occ, int64_t lin, i
     return len >= 32 ? bits : (bits & ((1u << len) - 1u));
 }
 
+// Exact int <-> float conversions of small integers by FP32 adds of 1.5 * 2^23 (the float whose mantissa
+// unit is 1): the FMA pipe runs them at the full FP32 rate, while this GPU executes the conversion
+// instructions on its FP64 pipe, at 1/64 of that rate.
+__device__ __forceinline__ float small_i2f(int32_t i) {  // |i| < 2^22
+    return __fsub_rn(__int_as_float(0x4B400000 + i), 12582912.0f);
+}
+__device__ __forceinline__ int32_t small_floor(float x) {  // floor(x), |x| < 2^22
+    return __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000;
+}
+// __uint2float_rn without a conversion instruction: the two 16-bit halves are exact floats, and the one
+// rounding of their sum is the rounding of x to nearest
+__device__ __forceinline__ float u32_to_float(uint32_t x) {
+    return __fadd_rn(__fmul_rn(small_i2f((int32_t)(x >> 16)), 65536.0f), small_i2f((int32_t)(x & 0xffffu)));
+}
+
 __device__ __forceinline__ float sqrt_approx(float x) {
     float y;
     asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -206,22 +222,35 @@ __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, 
     for (int r = 0; r < R; r++) {
         // rows in order of their nearest cell-to-cell distance: none after the first one beyond R2q
         if (rows_r2[r] > R2q) break;
-        const int8_t* row = rows + r * (D + 1);
+        // the row's D + 1 bytes in one load where they make a whole aligned word (D = 3, 7)
+        int8_t row[D + 1];
+        if constexpr (D + 1 == 4) {
+            const uint32_t wd = __ldg((const unsigned int*)(rows + r * 4));
+#pragma unroll
+            for (int j = 0; j < 4; j++) row[j] = (int8_t)(wd >> (8 * j));
+        } else if constexpr (D + 1 == 8) {
+            const uint2 wd = __ldg((const uint2*)(rows + r * 8));
+#pragma unroll
+            for (int j = 0; j < 8; j++) row[j] = (int8_t)((j < 4 ? wd.x : wd.y) >> (8 * (j & 3)));
+        } else {
+#pragma unroll
+            for (int j = 0; j <= D; j++) row[j] = rows[r * (D + 1) + j];
+        }
         int32_t olo, ohi;
         if (qo) {
             float rest = 0.f;
 #pragma unroll
             for (int d = 1; d < D; d++) {
                 const int32_t o = row[1 + d];
-                const float gap = o > 0 ? __fsub_rn(__fmul_rn((float)o, cf[d]), qo[d])
-                                        : (o < 0 ? __fsub_rn(qo[d], __fmul_rn((float)(o + 1), cf[d])) : 0.f);
+                const float gap = o > 0 ? __fsub_rn(__fmul_rn(small_i2f(o), cf[d]), qo[d])
+                                        : (o < 0 ? __fsub_rn(qo[d], __fmul_rn(small_i2f(o + 1), cf[d])) : 0.f);
                 rest = __fadd_rn(rest, __fmul_rn(gap, gap));
             }
             if (rest > R2q) continue;
             // dimension 0: offset o > 0 is within reach iff o c0 - q0 <= s, o < 0 iff q0 - (o + 1) c0 <= s
             const float sr = sqrt_approx(__fsub_rn(R2q, rest));
-            const int32_t up = __float2int_rd(__fmul_rn(__fadd_rn(sr, qo[0]), inv_c0));
-            const int32_t dn = -1 - __float2int_rd(__fmul_rn(__fsub_rn(sr, qo[0]), inv_c0));
+            const int32_t up = small_floor(__fmul_rn(__fadd_rn(sr, qo[0]), inv_c0));
+            const int32_t dn = -1 - small_floor(__fmul_rn(__fsub_rn(sr, qo[0]), inv_c0));
             olo = max((int32_t)row[0], min(dn, 0));
             ohi = min((int32_t)row[1], max(up, 0));
         } else {
@@ -230,7 +259,7 @@ __device__ __forceinline__ bool walk_rows(const int32_t* n, const int8_t* rows, 
             const float avail = R2q - rows_r2[r], c0sq = cf[0] * cf[0];
             const int32_t ext = 1 + max(-(int32_t)row[0], (int32_t)row[1]);
             int32_t o0max = 1;
-            while (o0max < ext && __fmul_rn((float)(o0max * o0max), c0sq) <= avail) o0max++;
+            while (o0max < ext && __fmul_rn(small_i2f(o0max * o0max), c0sq) <= avail) o0max++;
             olo = max((int32_t)row[0], -o0max);
             ohi = min((int32_t)row[1], o0max);
         }
@@ -331,7 +360,7 @@ template <int D>
 __device__ __forceinline__ void model_delta(const float* cf, const int32_t* o, const float* off_s, const float* off_q,
                                             float* dlt) {
 #pragma unroll
-    for (int d = 0; d < D; d++) dlt[d] = __fadd_rn(__fmul_rn((float)o[d], cf[d]), __fsub_rn(off_s[d], off_q[d]));
+    for (int d = 0; d < D; d++) dlt[d] = __fadd_rn(__fmul_rn(small_i2f(o[d]), cf[d]), __fsub_rn(off_s[d], off_q[d]));
 }
 
 template <int D>
@@ -369,6 +398,11 @@ __device__ __forceinline__ void fixed_cell(uint64_t a, uint64_t bits, uint32_t r
 __device__ __forceinline__ float search_r2(double rq, double rmax) {
     const float s = (float)(rq + rmax);
     return s * s * 1.0001f;
+}
+// the same from float radii, rounded up: no FP64 instruction (the 1e-4 margin is far above the radii's rounding)
+__device__ __forceinline__ float search_r2f(float rq, float rmax) {
+    const float s = __fadd_ru(rq, rmax);
+    return __fmul_ru(__fmul_ru(s, s), 1.0001f);
 }
 
 // Bit patterns of non-negative doubles order like the values: integer max / compare on the ALU

@@ -50,6 +50,7 @@ struct CandArgs {
     uint32_t* alive;    // candidates that survived the probe
     uint32_t* counters; // [0] = alive, [1] = accepted, [2] = error bits, [3] = gathered, [4] = FP64 retests
     float* off;         // FP32 screening offsets of the candidates (guard-band form)
+    float* radf;        // their radii in FP32, written by the probe for the candidates it keeps (guard-band form)
     int32_t* kc;        // cell coordinates of the candidates (guard-band form)
     int32_t* blk;       // NB lower-priority colliders per candidate
     uint8_t* nblk;

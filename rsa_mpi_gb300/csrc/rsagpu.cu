@@ -119,6 +119,7 @@ struct CandBuffers {
         dfree(a.nblk);
         dfree(a.gather);
         dfree(a.off);
+        dfree(a.radf);
         dfree(a.kc);
         dfree(vidx);
         cap = 0;
@@ -425,6 +426,7 @@ void ensure_cand(rsagpu_algo* A, uint64_t n) {
     C.a.nblk = dalloc<uint8_t>(cap);
     C.a.gather = dalloc<uint64_t>(cap);
     C.a.off = dalloc<float>(cap * D);
+    C.a.radf = dalloc<float>(cap);
     C.a.kc = dalloc<int32_t>(cap * D);
     C.vidx = dalloc<uint64_t>(cap);
     C.cap = cap;
