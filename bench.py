@@ -105,8 +105,10 @@ class ClockSampler:
 
 
 FORM_NAMES = {0: "plain FP64", 1: "FP32 screen + FP64 guard-band retest"}
-# the mask pass: one kernel per launch (FP32 form: the cooperative kernel at level 0, the per-lane walk below)
+# the mask pass: one kernel per launch (FP32 form: the cooperative kernel at level 0, the per-lane walk below);
+# FORM_TRAFFIC names its entry in profiles/refine_mask_traffic.json
 FORM_KERNEL = {0: "k_refine_mask", 1: "k_refine_mask32c (level 0) + k_refine_mask32"}
+FORM_TRAFFIC = {0: "k_refine_mask", 1: "mask_pass_fp32"}
 
 
 def aggregate(times, counts, dist=None, device="cpu"):
@@ -421,7 +423,7 @@ def main():
     traffic_path = os.path.join(ROOT, "profiles", "refine_mask_traffic.json")
     traffic, traffic_note = None, None
     if os.path.exists(traffic_path) and len(mask_vox):
-        tj = json.load(open(traffic_path)).get(FORM_KERNEL[args.form], {})
+        tj = json.load(open(traffic_path)).get(FORM_TRAFFIC[args.form], {})
         if tj.get("bytes_per_voxel"):
             traffic = float(tj["bytes_per_voxel"]) * float(np.mean(mask_vox))
             traffic_note = tj.get("note")

@@ -96,65 +96,45 @@ __host__ __device__ inline Geo<D> make_geo(const GridArgs& a) {
 inline unsigned nblocks(uint64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
 // ------------------------------------------------------------------------------------------------
-// level-0 voxel list: the lattice of getAllIndices (auxiliary/Loops.ixx:45-69) in Morton order
-// (morton_select); the list order is free (the reference's own order only matters to its own darts)
+// level-0 voxel list: the lattice of getAllIndices (auxiliary/Loops.ixx:45-69) in 2x..x2 block order
+// (block_order_coords); the list order is free (the reference's own order only matters to its own darts)
 // ------------------------------------------------------------------------------------------------
 struct NVox {
     int64_t n[D];
 };
 
-// Entry v of the lattice n[0] x .. x n[D-1] in Morton (Z) order: the coordinates' bits interleaved level
-// by level, dimension D-1 most significant within a level, the points outside the box skipped.  Found by
-// descending the implicit 2^D-tree: at each bit, the points of the current prefix with that bit 0 are
-// counted as a box intersected with the lattice.  Children are written in Morton order next to their
-// parent at every refinement (k_refine_write), so the list stays in Morton order at every level and any
-// few consecutive entries, however sparse the list, lie close together in space: the cooperative mask
-// pass (k_refine_mask32c) relies on it.
-__device__ __forceinline__ void morton_select(uint64_t v, const int64_t* n, int64_t* out) {
-    int L = 0;
+// Coordinates of entry v of the lattice n[0] x .. x n[D-1] listed block by block: blocks of 2 voxels per
+// dimension (1 at an odd upper edge) in lattice order, dimension 0 fastest, and the voxels of a block
+// dimension 0 fastest.  Any 8 consecutive entries of a 3D list form one 2x2x2 block, the group of the
+// cooperative level-0 mask pass (k_refine_mask32c).  (A full Morton order costs some 80 64-bit products per
+// voxel here, and the deeper levels, whose children are written next to their parent in either order,
+// measured no faster with it.)
+__device__ __forceinline__ void block_order_coords(uint64_t v, const int64_t* n, int64_t* out) {
+    uint64_t thick[D], blk[D], rem = v;
 #pragma unroll
-    for (int d = 0; d < D; d++)
-        while (L < 62 && (1ll << L) < n[d]) L++;
-    uint64_t f[D];
-    int nb[D];
+    for (int d = D - 1; d >= 0; d--) {
+        uint64_t t = 1, q = 1;
+#pragma unroll
+        for (int e = d + 1; e < D; e++) t *= thick[e];
+#pragma unroll
+        for (int e = 0; e < d; e++) q *= (uint64_t)n[e];
+        const uint64_t unit = 2 * t * q;  // entries of a slab two voxels thick along d
+        const uint64_t sl = rem / unit;
+        blk[d] = sl;
+        thick[d] = 2 * sl + 2 <= (uint64_t)n[d] ? 2 : 1;
+        rem -= sl * unit;
+    }
 #pragma unroll
     for (int d = 0; d < D; d++) {
-        f[d] = 0;
-        nb[d] = 0;
+        out[d] = (int64_t)(2 * blk[d] + rem % thick[d]);
+        rem /= thick[d];
     }
-    for (int l = L - 1; l >= 0; l--) {
-#pragma unroll
-        for (int d = D - 1; d >= 0; d--) {
-            uint64_t cnt = 1;
-#pragma unroll
-            for (int e = 0; e < D; e++) {
-                uint64_t fe = f[e];
-                int free_bits = L - nb[e];
-                if (e == d) {
-                    fe *= 2;
-                    free_bits -= 1;
-                }
-                const int64_t lo = (int64_t)(fe << free_bits), hi = (int64_t)((fe + 1) << free_bits);
-                const int64_t c = (hi < n[e] ? hi : n[e]) - lo;
-                cnt *= c > 0 ? (uint64_t)c : 0;
-            }
-            if (v < cnt) {
-                f[d] = 2 * f[d];
-            } else {
-                v -= cnt;
-                f[d] = 2 * f[d] + 1;
-            }
-            nb[d]++;
-        }
-    }
-#pragma unroll
-    for (int d = 0; d < D; d++) out[d] = (int64_t)f[d];
 }
 
 __global__ void k_vox_init(int64_t* vox, uint64_t V, NVox nv) {
     const uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
-    morton_select(v, nv.n, vox + v * D);
+    block_order_coords(v, nv.n, vox + v * D);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1253,7 +1233,7 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_mask32(Grid<D> g, Geo<D
 
 // ------------------------------------------------------------------------------------------------
 // Cooperative FP32 mask pass.  Groups of COOP_G consecutive voxels of the list (siblings, or neighbours in
-// the Morton order of the list) gather the occupied cells around their common box of cells once, into
+// the block order of the level-0 list) gather the occupied cells around their common box of cells once, into
 // shared memory, and every lane tests its own voxel against that list in step with the others: no per-lane
 // stencil walk with its divergent row loops.  A group whose voxels lie too far apart (union wider than one
 // occupancy window, more rows than COOP_ROWS_MAX or more than COOP_CAND spheres) takes the per-lane walk
@@ -1573,7 +1553,7 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
     int64_t cc[D];
 #pragma unroll
     for (int d = 0; d < D; d++) cc[d] = p.vin[v * D + d];
-    // children in Morton order (bit d of j = offset along d), which keeps the list in Morton order
+    // children in Morton order (bit d of j = offset along d): a 2x..x2 block, as the level-0 blocks
     for (int j = 0; j < CHILDREN; j++) {
         const int t = corner_of_child(j);
         if (!((mask[t >> 5] >> (t & 31)) & 1u)) continue;
@@ -1847,7 +1827,7 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
 
 void op_refine_mask(const GridArgs& ga, const RefineArgs& a, int f32, cudaStream_t s) {
     if (a.V == 0) return;
-    // Level 0 (one voxel per cell, neighbours in Morton order): 8-lane groups over their box of cells.  Deeper
+    // Level 0 (one voxel per cell, 2x2x2 blocks in the list): 8-lane groups over their box of cells.  Deeper
     // levels: the per-lane walk.  There the siblings share one cell and walk the same rows in step, and most
     // voxels are covered by a sphere of the first rows, where the walk stops; measured on the 3D r = 0.002
     // workload, a shared gather per cell (or a near-rows pass with the rest compacted) was slower.

@@ -33,7 +33,7 @@ __device__ __forceinline__ CandArgs with_lists(const CandArgs& c, const BInst& I
     return ci;
 }
 
-// level-0 voxels of every instance, in Morton order within each segment (as k_vox_init)
+// level-0 voxels of every instance, in block order within each segment (as k_vox_init)
 __global__ void k_b_vox_init(BatchArgs b, int64_t* vox) {
     const uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= b.V) return;
@@ -42,7 +42,7 @@ __global__ void k_b_vox_init(BatchArgs b, int64_t* vox) {
     int64_t n[D];
 #pragma unroll
     for (int d = 0; d < D; d++) n[d] = tab[s].nvox0[d];
-    morton_select(v - b.vox_off[s], n, vox + v * D);
+    block_order_coords(v - b.vox_off[s], n, vox + v * D);
 }
 
 // Slot t of the round holds global dart g = perm[t] (or t): dart (g - dart_off[s]) of instance s, under the
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(256) k_b_refine_write(BatchArgs b, RefineArgs 
         for (int d = 0; d < D; d++) a.vout[o * D + d] = cc[d];
         return;
     }
-    for (int j = 0; j < CHILDREN; j++) {  // Morton order, as k_refine_write
+    for (int j = 0; j < CHILDREN; j++) {  // as k_refine_write
         const int t = corner_of_child(j);
         if (!((mask[t >> 5] >> (t & 31)) & 1u)) continue;
 #pragma unroll
