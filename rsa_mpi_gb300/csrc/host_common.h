@@ -70,14 +70,33 @@ int guarded(F&& f) {
     }
 }
 
+// Device memory comes from the current device's stream-ordered pool, which keeps freed memory for reuse
+// (up to kPoolKeepBytes): a user's create / proceed / extract / destroy cycle then does not unmap and map
+// gigabytes each time (cudaFree of the 3D r = 0.002 buffers took 13.6 ms of a 225 ms call).  The
+// allocation is made on the legacy stream and waited for, and a free first waits for the device, as cudaMalloc
+// and cudaFree do, so every caller keeps their synchronous semantics.
+constexpr uint64_t kPoolKeepBytes = 128ull << 30;
+
+inline void keep_pool_memory() {
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = kPoolKeepBytes;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+}
+
 template <class T>
 T* dalloc(uint64_t n) {
     if (n == 0) n = 1;
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    keep_pool_memory();
+    cudaError_t e = cudaMallocAsync(&p, n * sizeof(T), 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        raise(RSAGPU_ERR_CUDA, "cudaMalloc of %llu bytes failed: %s", (unsigned long long)(n * sizeof(T)),
+        raise(RSAGPU_ERR_CUDA, "device allocation of %llu bytes failed: %s", (unsigned long long)(n * sizeof(T)),
               cudaGetErrorString(e));
     }
     return (T*)p;
@@ -85,7 +104,11 @@ T* dalloc(uint64_t n) {
 
 template <class T>
 void dfree(T*& p) {
-    if (p) cudaFree(p);
+    if (p) {
+        cudaDeviceSynchronize();  // no kernel in flight may still use p
+        cudaFreeAsync(p, 0);
+        cudaStreamSynchronize(0);
+    }
     p = nullptr;
 }
 
