@@ -78,6 +78,11 @@ __host__ __device__ inline Grid<D> make_grid(const GridArgs& a) {
     }
     g.guard = a.guard;
     g.mono = a.mono;
+    g.bocc = a.bocc;
+    for (int d = 0; d < D; d++) {
+        g.nb[d] = a.nb[d];
+        g.inv_cf[d] = (float)a.inv_c[d];
+    }
     g.rmono = a.rmono;
     g.rmonof = (float)a.rmono;
     g.rmaxf = (float)a.rmax;
@@ -363,7 +368,7 @@ __device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, 
         }
         float rf = __double2float_rn(r);
         asm volatile("" : "+f"(rf));  // not rematerialised in the loop below: the conversion runs on the FP64 pipe
-        hit = visit_placed_o<D>(g, k, offq, search_r2f(rf, g.rmaxf), [&](int64_t idx, const int32_t* o, const int8_t* q) {
+        hit = visit_placed_fo<D>(g, k, offq, search_r2f(rf, g.rmaxf), [&](int64_t idx, const int32_t* o, const int8_t* q) {
             const float rs = g.mono ? g.rmonof : g.radf[idx];
             const float R = __fadd_rn(rf, rs);
             const float R2 = __fmul_rn(R, R);
@@ -686,16 +691,24 @@ __device__ __forceinline__ bool commit_body(const Grid<D>& g, const Geo<D>& geo,
             const uint32_t old = atomicOr(g.occ + (idx >> 5), bit);
             if (old & bit) atomicOr(&c.counters[2], (uint32_t)ERR_DOUBLE_OCCUPANCY);
             int64_t rem = idx;
+            int64_t bidx = 0, bmul = 1;
+            int bbit = 0;
 #pragma unroll
             for (int d = 0; d < D; d++) {
                 const int32_t kd = (int32_t)(rem % g.n[d]);
                 rem /= g.n[d];
+                if (D == 3) {
+                    bidx += (kd >> 2) * bmul;
+                    bmul *= g.nb[d];
+                    bbit += (kd & 3) << (2 * d);
+                }
                 const double x = c.pos[(uint64_t)i * D + d];
                 g.pos[idx * D + d] = x;
                 // FP32 screening offset from the cell's corner (guard-band form)
                 const double base = __dadd_rn(geo.inf[d], __dmul_rn((double)kd, g.c[d]));
                 if (g.off) ((float*)g.off)[idx * D + d] = __double2float_rn(__dsub_rn(x, base));
             }
+            if (D == 3 && g.bocc) atomicOr((unsigned long long*)g.bocc + bidx, 1ull << bbit);
             // a one-radius grid without per-cell radius or phase arrays (batched instances) skips them
             if (g.rad) g.rad[idx] = c.rad[i];
             if (g.radf) ((float*)g.radf)[idx] = __double2float_rn(c.rad[i]);
@@ -1066,17 +1079,46 @@ __device__ __forceinline__ void children32(const Grid<D>& g, const RefineParams&
     bool band = false;
 #pragma unroll
     for (int w = 0; w < MASK_WORDS; w++) c32[w] = 0;
-    for (int t = 0; t < CHILDREN; t++) {
-        const int jb = child_bits(t);
-        float acc = 0.f;
+    if constexpr (CHILDREN <= 16) {
+        // the children's corner sums as a tree over the dimensions, in dimension order (the association of the
+        // per-child loop below, bit for bit): two squared terms per dimension instead of one per child (D <= 4:
+        // the 2^D partial sums stay in registers)
+        float acc[CHILDREN];
 #pragma unroll
         for (int d = 0; d < D; d++) {
-            const float dd = ((jb >> d) & 1) ? d1[d] : d0[d];
-            const float a = fmaxf(fabsf(dd), fabsf(__fsub_rn(p.nlenf[d], dd)));
-            acc = __fadd_rn(acc, __fmul_rn(a, a));
+            const float a0 = fmaxf(fabsf(d0[d]), fabsf(__fsub_rn(p.nlenf[d], d0[d])));
+            const float a1 = fmaxf(fabsf(d1[d]), fabsf(__fsub_rn(p.nlenf[d], d1[d])));
+            const float s0 = __fmul_rn(a0, a0), s1 = __fmul_rn(a1, a1);
+            if (d == 0) {
+                acc[0] = __fadd_rn(0.f, s0);
+                acc[1] = __fadd_rn(0.f, s1);
+            } else {
+#pragma unroll
+                for (int j = (1 << d) - 1; j >= 0; j--) {
+                    acc[j | (1 << d)] = __fadd_rn(acc[j], s1);
+                    acc[j] = __fadd_rn(acc[j], s0);
+                }
+            }
         }
-        if (acc < lo) c32[t >> 5] |= 1u << (t & 31);
-        else if (acc <= hi) band = true;
+#pragma unroll
+        for (int t = 0; t < CHILDREN; t++) {
+            const float x = acc[child_bits(t)];
+            if (x < lo) c32[0] |= 1u << t;
+            else if (x <= hi) band = true;
+        }
+    } else {
+        for (int t = 0; t < CHILDREN; t++) {
+            const int jb = child_bits(t);
+            float acc = 0.f;
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                const float dd = ((jb >> d) & 1) ? d1[d] : d0[d];
+                const float a = fmaxf(fabsf(dd), fabsf(__fsub_rn(p.nlenf[d], dd)));
+                acc = __fadd_rn(acc, __fmul_rn(a, a));
+            }
+            if (acc < lo) c32[t >> 5] |= 1u << (t & 31);
+            else if (acc <= hi) band = true;
+        }
     }
     if (band) {
         rt++;
@@ -1109,7 +1151,7 @@ __device__ __forceinline__ bool refine_mask32_body(const Grid<D>& g, const Geo<D
         int npre = 0;
         bool overflow = false;
         const float R2q = search_r2f(p.rminf, g.rmaxf);
-        const bool covered = visit_placed_o<D>(g, k, relc, R2q, [&](int64_t idx, const int32_t* o, const int8_t* q) {
+        const bool covered = visit_placed_fo<D>(g, k, relc, R2q, [&](int64_t idx, const int32_t* o, const int8_t* q) {
             visits++;
             const float rs = g.mono ? g.rmonof : g.radf[idx];
             float d0[D], d1[D];

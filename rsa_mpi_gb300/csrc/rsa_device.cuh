@@ -66,6 +66,9 @@ struct Grid {
     float cf[D];    // cell edge rounded to float
     float guard;    // bound on |FP32 model - FP64 value| of any squared distance the kernels compare
     int mono;       // one radius for every sphere
+    const unsigned long long* bocc;  // 3D: occupancy by 4x4x4 bricks of cells, or null
+    int32_t nb[D];                   // bricks per dimension
+    float inv_cf[D];                 // inverse cell edges
     double rmono;
     float rmonof;
 };
@@ -352,6 +355,75 @@ __device__ __forceinline__ bool visit_placed_o(const Grid<D>& g, const int32_t* 
         }
         return false;
     });
+}
+
+// Brick walk (3D grids with a brick map): the placed spheres in the cells within m_d cells of cell k, read as
+// 4x4x4 bricks of occupancy bits, 2 to 3 bricks per dimension, instead of stencil rows.  Cell-based (a
+// superset of the point-trimmed walk); only for neighbourhoods that do not wrap around the periodic box
+// (brick_reach returns false otherwise, and the caller walks the rows).  f(idx, o) returns true to stop.
+template <int D>
+__device__ __forceinline__ bool brick_reach(const Grid<D>& g, const int32_t* k, float R2q, int32_t* m) {
+    if (D != 3 || !g.bocc) return false;
+    const float s = sqrt_approx(R2q);
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        m[d] = 1 + small_floor(__fmul_rn(s, g.inv_cf[d]));
+        ok = ok && k[d] - m[d] >= 0 && k[d] + m[d] < g.n[d];
+    }
+    return ok;
+}
+
+template <int D, class F>
+__device__ __forceinline__ bool visit_bricks(const Grid<D>& g, const int32_t* k, const int32_t* m, F&& f) {
+    static_assert(D == 3, "bricks are 4x4x4");
+    const int32_t lo0 = k[0] - m[0], hi0 = k[0] + m[0];
+    const int32_t lo1 = k[1] - m[1], hi1 = k[1] + m[1];
+    const int32_t lo2 = k[2] - m[2], hi2 = k[2] + m[2];
+    auto span = [](int32_t lo, int32_t hi, int32_t b) {  // bits of cells [lo, hi] in brick b (4 cells)
+        const int32_t a = max(lo, 4 * b) - 4 * b, e = min(hi, 4 * b + 3) - 4 * b;
+        return ((1u << (e + 1)) - 1u) & ~((1u << a) - 1u);
+    };
+    for (int32_t bz = lo2 >> 2; bz <= (hi2 >> 2); bz++) {
+        const uint32_t zm = span(lo2, hi2, bz);
+        for (int32_t by = lo1 >> 2; by <= (hi1 >> 2); by++) {
+            const uint32_t ym = span(lo1, hi1, by);
+            for (int32_t bx = lo0 >> 2; bx <= (hi0 >> 2); bx++) {
+                const uint32_t xm = span(lo0, hi0, bx);
+                unsigned long long row = 0;
+#pragma unroll
+                for (int y = 0; y < 4; y++)
+                    if ((ym >> y) & 1u) row |= (unsigned long long)xm << (4 * y);
+                unsigned long long mask = 0;
+#pragma unroll
+                for (int z = 0; z < 4; z++)
+                    if ((zm >> z) & 1u) mask |= row << (16 * z);
+                unsigned long long bits = __ldg(g.bocc + (bx + (int64_t)g.nb[0] * (by + (int64_t)g.nb[1] * bz))) & mask;
+                while (bits) {
+                    const int j = __ffsll((long long)bits) - 1;
+                    bits &= bits - 1;
+                    const int32_t c0 = 4 * bx + (j & 3), c1 = 4 * by + ((j >> 2) & 3), c2 = 4 * bz + (j >> 4);
+                    const int32_t o[3] = {c0 - k[0], c1 - k[1], c2 - k[2]};
+                    const int64_t idx = c0 + (int64_t)g.n[0] * (c1 + (int64_t)g.n[1] * c2);
+                    if (f(idx, o)) return true;
+                }
+            }
+        }
+    }
+    return false;
+}
+
+// visit_placed_o by bricks where they apply, else by rows
+template <int D, class F>
+__device__ __forceinline__ bool visit_placed_fo(const Grid<D>& g, const int32_t* k, const float* qo, float R2q, F&& f) {
+    if constexpr (D == 3) {
+        int32_t m[D];
+        if (brick_reach<D>(g, k, R2q, m)) {
+            const int8_t q0[D] = {0, 0, 0};
+            return visit_bricks<D>(g, k, m, [&](int64_t idx, const int32_t* o) { return f(idx, o, q0); });
+        }
+    }
+    return visit_placed_o<D>(g, k, qo, R2q, f);
 }
 
 // FP32 model of (image of a stored centre) - (query point): o c + (off_s - off_q), with o the integer

@@ -34,6 +34,8 @@ struct GridArgs {
     float guard;         // guard band of the FP32 screen (absolute, on squared distances)
     int mono;            // one radius class
     double rmono;
+    unsigned long long* bocc;  // 3D: occupancy by 4x4x4 bricks of cells (bit x + 4 y + 16 z), or null
+    int32_t nb[MAX_D];         // bricks per dimension
 };
 
 struct CandArgs {

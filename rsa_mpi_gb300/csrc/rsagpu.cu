@@ -82,6 +82,7 @@ struct SphereGrid {
         dfree(a.off);
         dfree(a.radf);
         dfree(a.occ);
+        dfree(a.bocc);
         dfree(a.pos);
         dfree(a.rad);
         dfree(a.phase);
@@ -394,6 +395,17 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
     G.head = dalloc<int32_t>(ncells);
     G.cocc = dalloc<uint32_t>(nwords);
     CK(cudaMemset(a.occ, 0, nwords * sizeof(uint32_t)));
+    a.bocc = nullptr;
+    if (D == 3) {
+        // the same occupancy by 4x4x4 bricks (64 bits each), for the brick walks
+        uint64_t nbricks = 1;
+        for (int d = 0; d < D; d++) {
+            a.nb[d] = (a.n[d] + 3) / 4;
+            nbricks *= (uint64_t)a.nb[d];
+        }
+        a.bocc = dalloc<unsigned long long>(nbricks);
+        CK(cudaMemset(a.bocc, 0, nbricks * sizeof(unsigned long long)));
+    }
     CK(cudaMemset(G.cocc, 0, nwords * sizeof(uint32_t)));
     CK(cudaMemset(G.head, 0xFF, ncells * sizeof(int32_t)));
     G.ready = true;
