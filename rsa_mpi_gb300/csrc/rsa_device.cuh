@@ -361,25 +361,33 @@ __device__ __forceinline__ bool visit_placed_o(const Grid<D>& g, const int32_t* 
 // 4x4x4 bricks of occupancy bits, 2 to 3 bricks per dimension, instead of stencil rows.  Cell-based (a
 // superset of the point-trimmed walk); only for neighbourhoods that do not wrap around the periodic box
 // (brick_reach returns false otherwise, and the caller walks the rows).  f(idx, o) returns true to stop.
+// The cells [lo_d, hi_d] within reach sqrt(R2q) of the query: cell k at offset qo from its corner (the
+// reach along +d is the distance to the cell's upper face plus whole cells, along -d to its lower face), or
+// of any point of cell k when qo is null.  The 1e-4 margin of R2q covers the float error of these bounds.
 template <int D>
-__device__ __forceinline__ bool brick_reach(const Grid<D>& g, const int32_t* k, float R2q, int32_t* m) {
+__device__ __forceinline__ bool brick_reach(const Grid<D>& g, const int32_t* k, const float* qo, float R2q,
+                                            int32_t* lo, int32_t* hi) {
     if (D != 3 || !g.bocc) return false;
     const float s = sqrt_approx(R2q);
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < D; d++) {
-        m[d] = 1 + small_floor(__fmul_rn(s, g.inv_cf[d]));
-        ok = ok && k[d] - m[d] >= 0 && k[d] + m[d] < g.n[d];
+        const float up = qo ? __fsub_rn(s, __fsub_rn(g.cf[d], qo[d])) : s;  // beyond the upper face
+        const float dn = qo ? __fsub_rn(s, qo[d]) : s;                      // beyond the lower face
+        hi[d] = k[d] + (up < 0.f ? 0 : 1 + small_floor(__fmul_rn(up, g.inv_cf[d])));
+        lo[d] = k[d] - (dn < 0.f ? 0 : 1 + small_floor(__fmul_rn(dn, g.inv_cf[d])));
+        ok = ok && lo[d] >= 0 && hi[d] < g.n[d];
     }
     return ok;
 }
 
 template <int D, class F>
-__device__ __forceinline__ bool visit_bricks(const Grid<D>& g, const int32_t* k, const int32_t* m, F&& f) {
+__device__ __forceinline__ bool visit_bricks(const Grid<D>& g, const int32_t* k, const int32_t* lo, const int32_t* hi,
+                                             F&& f) {
     static_assert(D == 3, "bricks are 4x4x4");
-    const int32_t lo0 = k[0] - m[0], hi0 = k[0] + m[0];
-    const int32_t lo1 = k[1] - m[1], hi1 = k[1] + m[1];
-    const int32_t lo2 = k[2] - m[2], hi2 = k[2] + m[2];
+    const int32_t lo0 = lo[0], hi0 = hi[0];
+    const int32_t lo1 = lo[1], hi1 = hi[1];
+    const int32_t lo2 = lo[2], hi2 = hi[2];
     auto span = [](int32_t lo, int32_t hi, int32_t b) {  // bits of cells [lo, hi] in brick b (4 cells)
         const int32_t a = max(lo, 4 * b) - 4 * b, e = min(hi, 4 * b + 3) - 4 * b;
         return ((1u << (e + 1)) - 1u) & ~((1u << a) - 1u);
@@ -417,10 +425,10 @@ __device__ __forceinline__ bool visit_bricks(const Grid<D>& g, const int32_t* k,
 template <int D, class F>
 __device__ __forceinline__ bool visit_placed_fo(const Grid<D>& g, const int32_t* k, const float* qo, float R2q, F&& f) {
     if constexpr (D == 3) {
-        int32_t m[D];
-        if (brick_reach<D>(g, k, R2q, m)) {
+        int32_t lo[D], hi[D];
+        if (brick_reach<D>(g, k, qo, R2q, lo, hi)) {
             const int8_t q0[D] = {0, 0, 0};
-            return visit_bricks<D>(g, k, m, [&](int64_t idx, const int32_t* o) { return f(idx, o, q0); });
+            return visit_bricks<D>(g, k, lo, hi, [&](int64_t idx, const int32_t* o) { return f(idx, o, q0); });
         }
     }
     return visit_placed_o<D>(g, k, qo, R2q, f);
