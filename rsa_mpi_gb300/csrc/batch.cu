@@ -55,6 +55,7 @@ struct Inst {
 // device buffers of one wave; freed when it goes out of scope
 struct Wave {
     uint32_t* occ = nullptr;
+    unsigned long long* bocc = nullptr;  // 2D / 3D: brick occupancy of every instance
     double* pos = nullptr;
     float* off = nullptr;
     int32_t* head = nullptr;
@@ -89,6 +90,7 @@ struct Wave {
     uint64_t cand_cap = 0;
     ~Wave() {
         dfree(occ);
+        dfree(bocc);
         dfree(pos);
         dfree(off);
         dfree(head);
@@ -247,9 +249,14 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
     Events ev;
     // layout of the cell arrays and stencil rows
     std::vector<uint64_t> word_off(M + 1, 0), vox_off(M + 1, 0);
-    std::vector<uint64_t> rows_base(M), r2_base(M);
+    std::vector<uint64_t> rows_base(M), r2_base(M), brick_off(M + 1, 0);
     uint64_t rows_total = 0, r2_total = 0;
+    const bool bricks = D == 2 || D == 3;
+    const int side = D == 2 ? 8 : 4;  // bricks of 64 cells, as the single-instance grids
     for (uint32_t s = 0; s < M; s++) {
+        uint64_t nbr = 1;
+        for (int d = 0; d < D && bricks; d++) nbr *= (uint64_t)((I[s]->plan.a.n[d] + side - 1) / side);
+        brick_off[s + 1] = brick_off[s] + (bricks ? nbr : 0);
         word_off[s + 1] = word_off[s] + I[s]->cells / 32;
         vox_off[s + 1] = vox_off[s] + I[s]->V0;
         rows_base[s] = rows_total;
@@ -265,6 +272,10 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
     if (f32) W.off = dalloc<float>(ncells * D);
     W.head = dalloc<int32_t>(ncells);
     CK(cudaMemsetAsync(W.occ, 0, (nwords + 1) * sizeof(uint32_t), st));
+    if (bricks) {
+        W.bocc = dalloc<unsigned long long>(brick_off[M]);
+        CK(cudaMemsetAsync(W.bocc, 0, brick_off[M] * sizeof(unsigned long long), st));
+    }
     CK(cudaMemsetAsync(W.cocc, 0, (nwords + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(W.head, 0xFF, ncells * sizeof(int32_t), st));
     {
@@ -295,6 +306,8 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
         b.g.rows_r2 = W.rows_r2 + r2_base[s];
         b.g.mono = 1;
         b.g.rmono = I[s]->r;
+        b.g.bocc = bricks ? W.bocc + brick_off[s] : nullptr;
+        for (int d = 0; d < D && bricks; d++) b.g.nb[d] = (I[s]->plan.a.n[d] + side - 1) / side;
         b.head = W.head + cell0;
         b.cocc = W.cocc + word_off[s];
         b.seed = I[s]->seed;

@@ -693,14 +693,15 @@ __device__ __forceinline__ bool commit_body(const Grid<D>& g, const Geo<D>& geo,
             int64_t rem = idx;
             int64_t bidx = 0, bmul = 1;
             int bbit = 0;
+            constexpr int SB = brick_bits<D>();
 #pragma unroll
             for (int d = 0; d < D; d++) {
                 const int32_t kd = (int32_t)(rem % g.n[d]);
                 rem /= g.n[d];
-                if (D == 3) {
-                    bidx += (kd >> 2) * bmul;
+                if (D == 2 || D == 3) {
+                    bidx += (kd >> SB) * bmul;
                     bmul *= g.nb[d];
-                    bbit += (kd & 3) << (2 * d);
+                    bbit += (kd & ((1 << SB) - 1)) << (SB * d);
                 }
                 const double x = c.pos[(uint64_t)i * D + d];
                 g.pos[idx * D + d] = x;
@@ -708,7 +709,7 @@ __device__ __forceinline__ bool commit_body(const Grid<D>& g, const Geo<D>& geo,
                 const double base = __dadd_rn(geo.inf[d], __dmul_rn((double)kd, g.c[d]));
                 if (g.off) ((float*)g.off)[idx * D + d] = __double2float_rn(__dsub_rn(x, base));
             }
-            if (D == 3 && g.bocc) atomicOr((unsigned long long*)g.bocc + bidx, 1ull << bbit);
+            if ((D == 2 || D == 3) && g.bocc) atomicOr((unsigned long long*)g.bocc + bidx, 1ull << bbit);
             // a one-radius grid without per-cell radius or phase arrays (batched instances) skips them
             if (g.rad) g.rad[idx] = c.rad[i];
             if (g.radf) ((float*)g.radf)[idx] = __double2float_rn(c.rad[i]);

@@ -66,7 +66,7 @@ struct Grid {
     float cf[D];    // cell edge rounded to float
     float guard;    // bound on |FP32 model - FP64 value| of any squared distance the kernels compare
     int mono;       // one radius for every sphere
-    const unsigned long long* bocc;  // 3D: occupancy by 4x4x4 bricks of cells, or null
+    const unsigned long long* bocc;  // 2D / 3D: occupancy by bricks of 64 cells (8x8, 4x4x4), or null
     int32_t nb[D];                   // bricks per dimension
     float inv_cf[D];                 // inverse cell edges
     double rmono;
@@ -357,17 +357,21 @@ __device__ __forceinline__ bool visit_placed_o(const Grid<D>& g, const int32_t* 
     });
 }
 
-// Brick walk (3D grids with a brick map): the placed spheres in the cells within m_d cells of cell k, read as
-// 4x4x4 bricks of occupancy bits, 2 to 3 bricks per dimension, instead of stencil rows.  Cell-based (a
-// superset of the point-trimmed walk); only for neighbourhoods that do not wrap around the periodic box
-// (brick_reach returns false otherwise, and the caller walks the rows).  f(idx, o) returns true to stop.
+// Brick walk (2D and 3D grids with a brick map): the placed spheres in the cells within reach of the query, read
+// as bricks of 64 occupancy bits (8x8 cells in 2D, 4x4x4 in 3D; brick_bits per side), 1 to 3 bricks per
+// dimension, instead of stencil rows.  Cell-box based (a superset of the point-trimmed walk); only for
+// neighbourhoods that do not wrap around the periodic box (brick_reach returns false otherwise, and the caller
+// walks the rows).  f(idx, o) returns true to stop.
+template <int D>
+__host__ __device__ constexpr int brick_bits() { return D == 2 ? 3 : 2; }
+
 // The cells [lo_d, hi_d] within reach sqrt(R2q) of the query: cell k at offset qo from its corner (the
 // reach along +d is the distance to the cell's upper face plus whole cells, along -d to its lower face), or
 // of any point of cell k when qo is null.  The 1e-4 margin of R2q covers the float error of these bounds.
 template <int D>
 __device__ __forceinline__ bool brick_reach(const Grid<D>& g, const int32_t* k, const float* qo, float R2q,
                                             int32_t* lo, int32_t* hi) {
-    if (D != 3 || !g.bocc) return false;
+    if ((D != 2 && D != 3) || !g.bocc) return false;
     const float s = sqrt_approx(R2q);
     bool ok = true;
 #pragma unroll
@@ -381,38 +385,51 @@ __device__ __forceinline__ bool brick_reach(const Grid<D>& g, const int32_t* k, 
     return ok;
 }
 
+// bits of cells [lo, hi] within brick b of a side of 2^SB cells
+template <int SB>
+__device__ __forceinline__ uint32_t brick_span(int32_t lo, int32_t hi, int32_t b) {
+    const int32_t a = max(lo, b << SB) - (b << SB), e = min(hi, (b << SB) + (1 << SB) - 1) - (b << SB);
+    return ((2u << e) - 1u) & ~((1u << a) - 1u);
+}
+
 template <int D, class F>
 __device__ __forceinline__ bool visit_bricks(const Grid<D>& g, const int32_t* k, const int32_t* lo, const int32_t* hi,
                                              F&& f) {
-    static_assert(D == 3, "bricks are 4x4x4");
-    const int32_t lo0 = lo[0], hi0 = hi[0];
-    const int32_t lo1 = lo[1], hi1 = hi[1];
-    const int32_t lo2 = lo[2], hi2 = hi[2];
-    auto span = [](int32_t lo, int32_t hi, int32_t b) {  // bits of cells [lo, hi] in brick b (4 cells)
-        const int32_t a = max(lo, 4 * b) - 4 * b, e = min(hi, 4 * b + 3) - 4 * b;
-        return ((1u << (e + 1)) - 1u) & ~((1u << a) - 1u);
-    };
-    for (int32_t bz = lo2 >> 2; bz <= (hi2 >> 2); bz++) {
-        const uint32_t zm = span(lo2, hi2, bz);
-        for (int32_t by = lo1 >> 2; by <= (hi1 >> 2); by++) {
-            const uint32_t ym = span(lo1, hi1, by);
-            for (int32_t bx = lo0 >> 2; bx <= (hi0 >> 2); bx++) {
-                const uint32_t xm = span(lo0, hi0, bx);
+    static_assert(D == 2 || D == 3, "bricks of 8x8 or 4x4x4 cells");
+    constexpr int SB = brick_bits<D>(), SIDE = 1 << SB;
+    const int32_t lo2 = D == 3 ? lo[D == 3 ? 2 : 0] : 0, hi2 = D == 3 ? hi[D == 3 ? 2 : 0] : 0;
+    for (int32_t bz = lo2 >> SB; bz <= (hi2 >> SB); bz++) {
+        const uint32_t zm = D == 3 ? brick_span<SB>(lo2, hi2, bz) : 1u;
+        for (int32_t by = lo[1] >> SB; by <= (hi[1] >> SB); by++) {
+            const uint32_t ym = brick_span<SB>(lo[1], hi[1], by);
+            for (int32_t bx = lo[0] >> SB; bx <= (hi[0] >> SB); bx++) {
+                const uint32_t xm = brick_span<SB>(lo[0], hi[0], bx);
                 unsigned long long row = 0;
 #pragma unroll
-                for (int y = 0; y < 4; y++)
-                    if ((ym >> y) & 1u) row |= (unsigned long long)xm << (4 * y);
-                unsigned long long mask = 0;
+                for (int y = 0; y < SIDE; y++)
+                    if ((ym >> y) & 1u) row |= (unsigned long long)xm << (SIDE * y);
+                unsigned long long mask = row;
+                if (D == 3) {
+                    mask = 0;
 #pragma unroll
-                for (int z = 0; z < 4; z++)
-                    if ((zm >> z) & 1u) mask |= row << (16 * z);
-                unsigned long long bits = __ldg(g.bocc + (bx + (int64_t)g.nb[0] * (by + (int64_t)g.nb[1] * bz))) & mask;
+                    for (int z = 0; z < SIDE; z++)
+                        if ((zm >> z) & 1u) mask |= row << (SIDE * SIDE * z);
+                }
+                const int64_t word = bx + (int64_t)g.nb[0] * (by + (D == 3 ? (int64_t)g.nb[1] * bz : 0));
+                unsigned long long bits = __ldg(g.bocc + word) & mask;
                 while (bits) {
                     const int j = __ffsll((long long)bits) - 1;
                     bits &= bits - 1;
-                    const int32_t c0 = 4 * bx + (j & 3), c1 = 4 * by + ((j >> 2) & 3), c2 = 4 * bz + (j >> 4);
-                    const int32_t o[3] = {c0 - k[0], c1 - k[1], c2 - k[2]};
-                    const int64_t idx = c0 + (int64_t)g.n[0] * (c1 + (int64_t)g.n[1] * c2);
+                    int32_t c[D], o[D];
+                    c[0] = (bx << SB) + (j & (SIDE - 1));
+                    c[1] = (by << SB) + ((j >> SB) & (SIDE - 1));
+                    if (D == 3) c[D == 3 ? 2 : 0] = (bz << SB) + (j >> (2 * SB));
+                    int64_t idx = 0;
+#pragma unroll
+                    for (int d = D - 1; d >= 0; d--) {
+                        o[d] = c[d] - k[d];
+                        idx = idx * g.n[d] + c[d];
+                    }
                     if (f(idx, o)) return true;
                 }
             }
@@ -424,10 +441,10 @@ __device__ __forceinline__ bool visit_bricks(const Grid<D>& g, const int32_t* k,
 // visit_placed_o by bricks where they apply, else by rows
 template <int D, class F>
 __device__ __forceinline__ bool visit_placed_fo(const Grid<D>& g, const int32_t* k, const float* qo, float R2q, F&& f) {
-    if constexpr (D == 3) {
+    if constexpr (D == 2 || D == 3) {
         int32_t lo[D], hi[D];
         if (brick_reach<D>(g, k, qo, R2q, lo, hi)) {
-            const int8_t q0[D] = {0, 0, 0};
+            const int8_t q0[D] = {};
             return visit_bricks<D>(g, k, lo, hi, [&](int64_t idx, const int32_t* o) { return f(idx, o, q0); });
         }
     }

@@ -396,11 +396,12 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
     G.cocc = dalloc<uint32_t>(nwords);
     CK(cudaMemset(a.occ, 0, nwords * sizeof(uint32_t)));
     a.bocc = nullptr;
-    if (D == 3) {
-        // the same occupancy by 4x4x4 bricks (64 bits each), for the brick walks
+    if (D == 2 || D == 3) {
+        // the same occupancy by bricks of 64 cells (8x8, 4x4x4), for the brick walks
+        const int side = D == 2 ? 8 : 4;
         uint64_t nbricks = 1;
         for (int d = 0; d < D; d++) {
-            a.nb[d] = (a.n[d] + 3) / 4;
+            a.nb[d] = (a.n[d] + side - 1) / side;
             nbricks *= (uint64_t)a.nb[d];
         }
         a.bocc = dalloc<unsigned long long>(nbricks);
