@@ -1571,6 +1571,243 @@ __global__ void __launch_bounds__(COOP_BLOCK) k_refine_mask32c(Grid<D> g, Geo<D>
     mask_epilogue(p, v, active, mask, survived, visits, rt);
 }
 
+// ------------------------------------------------------------------------------------------------
+// Warp-queue FP32 mask pass (3D grids with a brick map, levels >= 1).  In the per-lane walk each lane loops
+// over its own occupied cells and its own prefilter spheres, loops of very different lengths: 10 of 32 lanes
+// were active per instruction.  Here each lane puts its (voxel, occupied cell) pairs of 8 brick slots into a
+// queue in shared memory, and the 32 lanes of the warp test the queued pairs together (pair32): coverage as a
+// bit per voxel, prefilter spheres into a list per voxel.  The children of the uncovered voxels' prefilter
+// spheres are tested the same way (children32), the child masks ORed per voxel.  The set of pairs each voxel
+// gets is the set its own brick walk visits, and covering, the prefilter set and the child masks do not depend
+// on the order of the tests: the decisions are those of k_refine_mask32.  A voxel whose neighbourhood wraps
+// around the box, spans 3 bricks in a dimension, or has more than Q_PRE prefilter spheres takes the per-lane
+// walk.
+// ------------------------------------------------------------------------------------------------
+constexpr int Q_WARPS = 4;
+constexpr int Q_BLOCK = 32 * Q_WARPS;
+constexpr int Q_CAP = 160;  // queued (voxel, cell) pairs per warp
+constexpr int Q_PRE = 16;   // prefilter spheres kept per voxel
+constexpr int QD2 = D > 2 ? 2 : 0;  // the third dimension's index (this kernel runs for D = 3 only)
+
+struct WarpQueue {
+    float relc[D][32], relo[D][32];
+    uint32_t qcell[Q_CAP];
+    int8_t qo[D][Q_CAP];
+    uint8_t qown[Q_CAP];
+    uint32_t pcell[32][Q_PRE];
+    int8_t po[32][Q_PRE][D];
+    uint32_t npre[32];
+    uint32_t pref[32];  // inclusive prefix of the children phase's per-lane counts
+    uint32_t cov[32];
+    uint32_t covered;   // bit per lane: voxel covered
+    uint32_t over;      // bit per lane: prefilter list overflow
+};
+
+__global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> geo, RefineParams p) {
+    __shared__ WarpQueue wq[Q_WARPS];
+    const int lane = threadIdx.x & 31;
+    WarpQueue& Q = wq[threadIdx.x >> 5];
+    const uint64_t v = (uint64_t)blockIdx.x * Q_BLOCK + threadIdx.x;
+    const uint64_t vbase = v - lane;
+    const bool active = v < p.V;
+    int64_t cc[D];
+    int32_t k[D], lo[D], hi[D];
+    float relc[D], relo[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        cc[d] = active ? p.vin[v * D + d] : 0;
+        k[d] = lo[d] = hi[d] = 0;
+        relc[d] = relo[d] = 0.f;
+    }
+    if (active) voxel_query32(g, p, cc, k, relc, relo);
+    const float R2q = search_r2f(p.rminf, g.rmaxf);
+    bool mine = active && brick_reach<D>(g, k, relc, R2q, lo, hi);
+#pragma unroll
+    for (int d = 0; d < D; d++) mine = mine && (hi[d] >> 2) - (lo[d] >> 2) <= 1;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        Q.relc[d][lane] = relc[d];
+        Q.relo[d][lane] = relo[d];
+    }
+    Q.npre[lane] = 0;
+    Q.cov[lane] = 0;
+    if (lane == 0) {
+        Q.covered = 0;
+        Q.over = 0;
+    }
+    __syncwarp();
+    uint32_t rt = 0, visits = 0;
+    // the voxel of lane `own`, for the guard band's FP64 retests (loaded only there)
+    int64_t occ[D];
+    const Exact64 ex{g, geo, p, occ};
+    auto test_pair = [&](int own, uint32_t idx, const int32_t* o) {
+        float oc[D], oo[D], offs[D], d0[D], d1[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            oc[d] = Q.relc[d][own];
+            oo[d] = Q.relo[d][own];
+            offs[d] = g.off[(uint64_t)idx * D + d];
+        }
+        const float rs = g.mono ? g.rmonof : g.radf[idx];
+        const int r = pair32(g, p, ex, o, offs, rs, oc, oo, d0, d1,
+                             [&](int64_t& i2, int8_t* q2) {
+                                 i2 = idx;
+#pragma unroll
+                                 for (int d = 0; d < D; d++) {
+                                     q2[d] = 0;
+                                     occ[d] = p.vin[(vbase + own) * D + d];
+                                 }
+                             }, rt);
+        if (r == PAIR_COVERS) {
+            atomicOr(&Q.covered, 1u << own);
+        } else if (r == PAIR_PRE) {
+            const uint32_t sl = atomicAdd(&Q.npre[own], 1u);
+            if (sl < Q_PRE) {
+                Q.pcell[own][sl] = idx;
+#pragma unroll
+                for (int d = 0; d < D; d++) Q.po[own][sl][d] = (int8_t)o[d];
+            } else {
+                atomicOr(&Q.over, 1u << own);
+            }
+        }
+    };
+    uint32_t fill = 0;  // warp-uniform
+    auto flush = [&]() {
+        for (uint32_t e = lane; e < fill; e += 32) {
+            const int own = Q.qown[e];
+            if ((*(volatile uint32_t*)&Q.covered >> own) & 1u) continue;
+            int32_t o[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) o[d] = Q.qo[d][e];
+            visits++;
+            test_pair(own, Q.qcell[e], o);
+        }
+        __syncwarp();
+        fill = 0;
+    };
+    // visit phase: the (up to) 2 x 2 x 2 bricks of each voxel's range
+    for (int sl = 0; sl < 8; sl++) {
+        unsigned long long bits = 0;
+        int32_t b[D];
+        if (mine) {
+            b[0] = (lo[0] >> 2) + (sl & 1);
+            b[1] = (lo[1] >> 2) + ((sl >> 1) & 1);
+            b[QD2] = (lo[QD2] >> 2) + (sl >> 2);
+            if (b[0] <= (hi[0] >> 2) && b[1] <= (hi[1] >> 2) && b[QD2] <= (hi[QD2] >> 2)) {
+                const uint32_t xm = brick_span<2>(lo[0], hi[0], b[0]);
+                const uint32_t ym = brick_span<2>(lo[1], hi[1], b[1]);
+                const uint32_t zm = brick_span<2>(lo[QD2], hi[QD2], b[QD2]);
+                unsigned long long row = 0, mask = 0;
+#pragma unroll
+                for (int y = 0; y < 4; y++)
+                    if ((ym >> y) & 1u) row |= (unsigned long long)xm << (4 * y);
+#pragma unroll
+                for (int z = 0; z < 4; z++)
+                    if ((zm >> z) & 1u) mask |= row << (16 * z);
+                bits = __ldg(g.bocc + (b[0] + (int64_t)g.nb[0] * (b[1] + (int64_t)g.nb[1] * b[QD2]))) & mask;
+                if ((Q.covered >> lane) & 1u) bits = 0;  // covered already: no more pairs
+            }
+        }
+        const uint32_t c = __popcll(bits);
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+        if (fill + tot > Q_CAP) flush();
+        if (tot <= Q_CAP) {
+            uint32_t pos = fill + incl - c;
+            while (bits) {
+                const int j = __ffsll((long long)bits) - 1;
+                bits &= bits - 1;
+                const int32_t c0 = (b[0] << 2) + (j & 3), c1 = (b[1] << 2) + ((j >> 2) & 3), c2 = (b[QD2] << 2) + (j >> 4);
+                Q.qcell[pos] = (uint32_t)(c0 + g.n[0] * (c1 + g.n[1] * c2));
+                Q.qo[0][pos] = (int8_t)(c0 - k[0]);
+                Q.qo[1][pos] = (int8_t)(c1 - k[1]);
+                Q.qo[QD2][pos] = (int8_t)(c2 - k[QD2]);
+                Q.qown[pos] = (uint8_t)lane;
+                pos++;
+            }
+            fill += tot;
+            __syncwarp();
+        } else {
+            // more pairs than the queue holds: this slot lane by lane
+            while (bits) {
+                const int j = __ffsll((long long)bits) - 1;
+                bits &= bits - 1;
+                const int32_t c0 = (b[0] << 2) + (j & 3), c1 = (b[1] << 2) + ((j >> 2) & 3), c2 = (b[QD2] << 2) + (j >> 4);
+                int32_t o[D];
+                o[0] = c0 - k[0];
+                o[1] = c1 - k[1];
+                o[QD2] = c2 - k[QD2];
+                visits++;
+                test_pair(lane, (uint32_t)(c0 + g.n[0] * (c1 + g.n[1] * c2)), o);
+            }
+            __syncwarp();
+        }
+    }
+    flush();
+    // children phase: the (voxel, prefilter sphere) pairs of the uncovered voxels, over the warp
+    const uint32_t covered = Q.covered, over = Q.over;
+    const bool live = mine && !((covered >> lane) & 1u) && !((over >> lane) & 1u);
+    const uint32_t cnt = live ? min(Q.npre[lane], (uint32_t)Q_PRE) : 0u;
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    Q.pref[lane] = incl;
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    for (uint32_t e = lane; e < total; e += 32) {
+        int own = 0;  // the lane whose inclusive prefix first exceeds e
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (Q.pref[own + step - 1] <= e) own += step;
+        const uint32_t sl = e - (own ? Q.pref[own - 1] : 0u);
+        const uint32_t idx = Q.pcell[own][sl];
+        int32_t o[D];
+        float oc[D], oo[D], offs[D], d0[D], d1[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            o[d] = Q.po[own][sl][d];
+            oc[d] = Q.relc[d][own];
+            oo[d] = Q.relo[d][own];
+            offs[d] = g.off[(uint64_t)idx * D + d];
+        }
+        model_delta<D>(g.cf, o, offs, oc, d1);
+        model_delta<D>(g.cf, o, offs, oo, d0);
+        uint32_t c32[MASK_WORDS];
+        children32(g, p, ex, d0, d1, g.mono ? g.rmonof : g.radf[idx],
+                   [&](int64_t& i2, int8_t* q2) {
+                       i2 = idx;
+#pragma unroll
+                       for (int d = 0; d < D; d++) {
+                           q2[d] = 0;
+                           occ[d] = p.vin[(vbase + own) * D + d];
+                       }
+                   }, c32, rt);
+        atomicOr(&Q.cov[own], c32[0]);
+    }
+    __syncwarp();
+    uint32_t mask[MASK_WORDS];
+#pragma unroll
+    for (int w2 = 0; w2 < MASK_WORDS; w2++) mask[w2] = 0;
+    bool survived = false;
+    if (live) {
+        survived = true;
+        const uint32_t all = CHILDREN >= 32 ? 0xffffffffu : ((1u << CHILDREN) - 1u);
+        mask[0] = ~Q.cov[lane] & all;
+    } else if (active && !(mine && ((covered >> lane) & 1u))) {
+        // outside the brick walk's reach, or a prefilter list overflow: the per-lane walk
+        survived = refine_mask32_body(g, geo, p, cc, mask, visits, rt);
+    }
+    mask_epilogue(p, v, active, mask, survived, visits, rt);
+}
+
 __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
     const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
     uint32_t mask[MASK_WORDS];
@@ -1876,6 +2113,8 @@ void op_refine_mask(const GridArgs& ga, const RefineArgs& a, int f32, cudaStream
     // workload, a shared gather per cell (or a near-rows pass with the rest compacted) was slower.
     if (f32 && a.level == 0) {
         k_refine_mask32c<<<nblocks(a.V, COOP_BLOCK), COOP_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
+    } else if (f32 && D == 3 && ga.bocc && ga.ncells < (1ll << 32)) {
+        k_refine_mask32q<<<nblocks(a.V, Q_BLOCK), Q_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
     } else if (f32) {
         k_refine_mask32<<<nblocks(a.V, REFINE_BLOCK), REFINE_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
     }
