@@ -1591,9 +1591,9 @@ constexpr int QD2 = D > 2 ? 2 : 0;  // the third dimension's index (this kernel 
 
 struct WarpQueue {
     float relc[D][32], relo[D][32];
-    uint32_t qcell[Q_CAP];
-    int8_t qo[D][Q_CAP];
-    uint8_t qown[Q_CAP];
+    // one queued pair per word: cell index (bits 0-31), cell offsets + 128 (8 bits each, from bit 32), owner
+    // lane (bits 56-63)
+    unsigned long long q[Q_CAP];
     uint32_t pcell[32][Q_PRE];
     int8_t po[32][Q_PRE][D];
     uint32_t npre[32];
@@ -1674,13 +1674,14 @@ __global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> ge
     uint32_t fill = 0;  // warp-uniform
     auto flush = [&]() {
         for (uint32_t e = lane; e < fill; e += 32) {
-            const int own = Q.qown[e];
+            const unsigned long long w = Q.q[e];
+            const int own = (int)(w >> 56);
             if ((*(volatile uint32_t*)&Q.covered >> own) & 1u) continue;
             int32_t o[D];
 #pragma unroll
-            for (int d = 0; d < D; d++) o[d] = Q.qo[d][e];
+            for (int d = 0; d < D; d++) o[d] = (int32_t)((w >> (32 + 8 * d)) & 0xffu) - 128;
             visits++;
-            test_pair(own, Q.qcell[e], o);
+            test_pair(own, (uint32_t)w, o);
         }
         __syncwarp();
         fill = 0;
@@ -1723,11 +1724,10 @@ __global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> ge
                 const int j = __ffsll((long long)bits) - 1;
                 bits &= bits - 1;
                 const int32_t c0 = (b[0] << 2) + (j & 3), c1 = (b[1] << 2) + ((j >> 2) & 3), c2 = (b[QD2] << 2) + (j >> 4);
-                Q.qcell[pos] = (uint32_t)(c0 + g.n[0] * (c1 + g.n[1] * c2));
-                Q.qo[0][pos] = (int8_t)(c0 - k[0]);
-                Q.qo[1][pos] = (int8_t)(c1 - k[1]);
-                Q.qo[QD2][pos] = (int8_t)(c2 - k[QD2]);
-                Q.qown[pos] = (uint8_t)lane;
+                const uint32_t cell = (uint32_t)(c0 + g.n[0] * (c1 + g.n[1] * c2));
+                const uint32_t offs = (uint32_t)(c0 - k[0] + 128) | ((uint32_t)(c1 - k[1] + 128) << 8) |
+                                      ((uint32_t)(c2 - k[QD2] + 128) << 16) | ((uint32_t)lane << 24);
+                Q.q[pos] = (unsigned long long)cell | ((unsigned long long)offs << 32);
                 pos++;
             }
             fill += tot;
