@@ -1603,19 +1603,19 @@ struct WarpQueue {
     uint32_t over;      // bit per lane: prefilter list overflow
 };
 
-__global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> geo, RefineParams p) {
-    __shared__ WarpQueue wq[Q_WARPS];
+// The warp-queue pass for the 32 voxels of a warp, all lanes together (every lane calls it, active or not,
+// with the same grid): fills mask, returns true when this lane's voxel survives.  vin and vbase locate the
+// warp's voxels (their coordinates are reloaded for the guard band's retests).
+__device__ __forceinline__ bool mask32q_warp(const Grid<D>& g, const Geo<D>& geo, const RefineParams& p,
+                                             WarpQueue& Q, const int64_t* vin, uint64_t vbase, bool active,
+                                             const int64_t* cc_in, uint32_t* mask, uint32_t& visits, uint32_t& rt) {
     const int lane = threadIdx.x & 31;
-    WarpQueue& Q = wq[threadIdx.x >> 5];
-    const uint64_t v = (uint64_t)blockIdx.x * Q_BLOCK + threadIdx.x;
-    const uint64_t vbase = v - lane;
-    const bool active = v < p.V;
     int64_t cc[D];
     int32_t k[D], lo[D], hi[D];
     float relc[D], relo[D];
 #pragma unroll
     for (int d = 0; d < D; d++) {
-        cc[d] = active ? p.vin[v * D + d] : 0;
+        cc[d] = cc_in[d];
         k[d] = lo[d] = hi[d] = 0;
         relc[d] = relo[d] = 0.f;
     }
@@ -1636,7 +1636,6 @@ __global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> ge
         Q.over = 0;
     }
     __syncwarp();
-    uint32_t rt = 0, visits = 0;
     // the voxel of lane `own`, for the guard band's FP64 retests (loaded only there)
     int64_t occ[D];
     const Exact64 ex{g, geo, p, occ};
@@ -1655,7 +1654,7 @@ __global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> ge
 #pragma unroll
                                  for (int d = 0; d < D; d++) {
                                      q2[d] = 0;
-                                     occ[d] = p.vin[(vbase + own) * D + d];
+                                     occ[d] = vin[(vbase + own) * D + d];
                                  }
                              }, rt);
         if (r == PAIR_COVERS) {
@@ -1787,13 +1786,12 @@ __global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> ge
 #pragma unroll
                        for (int d = 0; d < D; d++) {
                            q2[d] = 0;
-                           occ[d] = p.vin[(vbase + own) * D + d];
+                           occ[d] = vin[(vbase + own) * D + d];
                        }
                    }, c32, rt);
         atomicOr(&Q.cov[own], c32[0]);
     }
     __syncwarp();
-    uint32_t mask[MASK_WORDS];
 #pragma unroll
     for (int w2 = 0; w2 < MASK_WORDS; w2++) mask[w2] = 0;
     bool survived = false;
@@ -1805,8 +1803,23 @@ __global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> ge
         // outside the brick walk's reach, or a prefilter list overflow: the per-lane walk
         survived = refine_mask32_body(g, geo, p, cc, mask, visits, rt);
     }
+    __syncwarp();
+    return survived;
+}
+
+__global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> geo, RefineParams p) {
+    __shared__ WarpQueue wq[Q_WARPS];
+    const uint64_t v = (uint64_t)blockIdx.x * Q_BLOCK + threadIdx.x;
+    const bool active = v < p.V;
+    int64_t cc[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) cc[d] = active ? p.vin[v * D + d] : 0;
+    uint32_t mask[MASK_WORDS], visits = 0, rt = 0;
+    const bool survived = mask32q_warp(g, geo, p, wq[threadIdx.x >> 5], p.vin, v - (threadIdx.x & 31), active, cc,
+                                       mask, visits, rt);
     mask_epilogue(p, v, active, mask, survived, visits, rt);
 }
+
 
 __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
     const uint64_t v = (uint64_t)blockIdx.x * REFINE_BLOCK + threadIdx.x;
