@@ -323,8 +323,9 @@ __device__ __forceinline__ void lazy_position(const Geo<D>& geo, const CandArgs&
 // (remove_collisions_with_validated_spheres, operator_cells_and_data_storage.ixx:54-76); the
 // others are linked into the candidate cell lists and appended to the alive list.
 // ------------------------------------------------------------------------------------------------
-// Probe of undecided candidate i; returns true when it stays alive (linked into the cell lists).
-template <bool F32>
+// Probe of undecided candidate i; returns true when it stays alive (linked into the cell lists).  OWN_FIRST
+// (FP32 form, one radius class) walks the dart's own brick first: 97 % of the darts die, most at a near sphere.
+template <bool F32, bool OWN_FIRST = false>
 __device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, uint32_t i,
                                            uint32_t& rt) {
     const double r = c.rad[i];
@@ -368,7 +369,7 @@ __device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, 
         }
         float rf = __double2float_rn(r);
         asm volatile("" : "+f"(rf));  // not rematerialised in the loop below: the conversion runs on the FP64 pipe
-        hit = visit_placed_fo<D>(g, k, offq, search_r2f(rf, g.rmaxf), [&](int64_t idx, const int32_t* o, const int8_t* q) {
+        hit = visit_placed_fo<D, OWN_FIRST>(g, k, offq, search_r2f(rf, g.rmaxf), [&](int64_t idx, const int32_t* o, const int8_t* q) {
             const float rs = g.mono ? g.rmonof : g.radf[idx];
             const float R = __fadd_rn(rf, rs);
             const float R2 = __fmul_rn(R, R);
@@ -408,11 +409,11 @@ __device__ __forceinline__ bool probe_body(const Grid<D>& g, const Geo<D>& geo, 
     return true;
 }
 
-template <bool F32>
+template <bool F32, bool OWN_FIRST = false>
 __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t rt = 0;
-    const bool alive = i < c.n && c.state[i] == ST_UNDECIDED && probe_body<F32>(g, geo, c, i, rt);
+    const bool alive = i < c.n && c.state[i] == ST_UNDECIDED && probe_body<F32, OWN_FIRST>(g, geo, c, i, rt);
     const uint32_t slot = warp_append(&c.counters[0], alive);
     if (alive) c.alive[slot] = i;
     if (F32) {
@@ -2049,7 +2050,8 @@ void op_darts32(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaSt
 
 void op_probe(const GridArgs& ga, const CandArgs& c, int f32, cudaStream_t s) {
     if (c.n == 0) return;
-    if (f32) k_probe<true><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    if (f32 && ga.mono) k_probe<true, true><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    else if (f32) k_probe<true><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
     else k_probe<false><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
     count_launch();
 }

@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(512, 2) k_b_probe(BatchArgs b, CandArgs c) {
         const BInst& I = ((const BInst*)b.table)[s];
         const Grid<D>& g = I.g;
         const Geo<D>& geo = I.geo;
-        alive = probe_body<F32>(g, geo, with_instance(c, b, I, s), i, rt);
+        alive = probe_body<F32, F32>(g, geo, with_instance(c, b, I, s), i, rt);  // one radius per instance
     }
     const uint32_t slot = warp_append(&c.counters[0], alive);
     if (alive) c.alive[slot] = i;

@@ -392,17 +392,30 @@ __device__ __forceinline__ uint32_t brick_span(int32_t lo, int32_t hi, int32_t b
     return ((2u << e) - 1u) & ~((1u << a) - 1u);
 }
 
-template <int D, class F>
+// the brick visited at step a of the ascending walk a = b0, b0 + 1, ...: brick a itself, or (OWN_FIRST) brick
+// `own` first, then the others ascending
+template <bool OWN_FIRST>
+__device__ __forceinline__ int32_t brick_at(int32_t b0, int32_t own, int32_t a) {
+    if (!OWN_FIRST) return a;
+    if (a == b0) return own;
+    return a - 1 < own ? a - 1 : a;
+}
+
+template <int D, bool OWN_FIRST = false, class F>
 __device__ __forceinline__ bool visit_bricks(const Grid<D>& g, const int32_t* k, const int32_t* lo, const int32_t* hi,
                                              F&& f) {
     static_assert(D == 2 || D == 3, "bricks of 8x8 or 4x4x4 cells");
     constexpr int SB = brick_bits<D>(), SIDE = 1 << SB;
-    const int32_t lo2 = D == 3 ? lo[D == 3 ? 2 : 0] : 0, hi2 = D == 3 ? hi[D == 3 ? 2 : 0] : 0;
-    for (int32_t bz = lo2 >> SB; bz <= (hi2 >> SB); bz++) {
+    constexpr int Z = D == 3 ? 2 : 0;
+    const int32_t lo2 = D == 3 ? lo[Z] : 0, hi2 = D == 3 ? hi[Z] : 0;
+    for (int32_t az = lo2 >> SB; az <= (hi2 >> SB); az++) {
+        const int32_t bz = brick_at<OWN_FIRST>(lo2 >> SB, D == 3 ? k[Z] >> SB : 0, az);
         const uint32_t zm = D == 3 ? brick_span<SB>(lo2, hi2, bz) : 1u;
-        for (int32_t by = lo[1] >> SB; by <= (hi[1] >> SB); by++) {
+        for (int32_t ay = lo[1] >> SB; ay <= (hi[1] >> SB); ay++) {
+            const int32_t by = brick_at<OWN_FIRST>(lo[1] >> SB, k[1] >> SB, ay);
             const uint32_t ym = brick_span<SB>(lo[1], hi[1], by);
-            for (int32_t bx = lo[0] >> SB; bx <= (hi[0] >> SB); bx++) {
+            for (int32_t ax = lo[0] >> SB; ax <= (hi[0] >> SB); ax++) {
+                const int32_t bx = brick_at<OWN_FIRST>(lo[0] >> SB, k[0] >> SB, ax);
                 const uint32_t xm = brick_span<SB>(lo[0], hi[0], bx);
                 unsigned long long row = 0;
 #pragma unroll
@@ -438,14 +451,16 @@ __device__ __forceinline__ bool visit_bricks(const Grid<D>& g, const int32_t* k,
     return false;
 }
 
-// visit_placed_o by bricks where they apply, else by rows
-template <int D, class F>
+// visit_placed_o by bricks where they apply, else by rows; OWN_FIRST visits the query's own brick first in each
+// dimension (a walk that stops at its first hit meets the near spheres sooner)
+template <int D, bool OWN_FIRST = false, class F>
 __device__ __forceinline__ bool visit_placed_fo(const Grid<D>& g, const int32_t* k, const float* qo, float R2q, F&& f) {
     if constexpr (D == 2 || D == 3) {
         int32_t lo[D], hi[D];
         if (brick_reach<D>(g, k, qo, R2q, lo, hi)) {
             const int8_t q0[D] = {};
-            return visit_bricks<D>(g, k, lo, hi, [&](int64_t idx, const int32_t* o) { return f(idx, o, q0); });
+            return visit_bricks<D, OWN_FIRST>(g, k, lo, hi,
+                                              [&](int64_t idx, const int32_t* o) { return f(idx, o, q0); });
         }
     }
     return visit_placed_o<D>(g, k, qo, R2q, f);
