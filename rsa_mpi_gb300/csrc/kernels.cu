@@ -1698,13 +1698,7 @@ __device__ __forceinline__ bool mask32q_warp(const Grid<D>& g, const Geo<D>& geo
                 const uint32_t xm = brick_span<2>(lo[0], hi[0], b[0]);
                 const uint32_t ym = brick_span<2>(lo[1], hi[1], b[1]);
                 const uint32_t zm = brick_span<2>(lo[QD2], hi[QD2], b[QD2]);
-                unsigned long long row = 0, mask = 0;
-#pragma unroll
-                for (int y = 0; y < 4; y++)
-                    if ((ym >> y) & 1u) row |= (unsigned long long)xm << (4 * y);
-#pragma unroll
-                for (int z = 0; z < 4; z++)
-                    if ((zm >> z) & 1u) mask |= row << (16 * z);
+                const unsigned long long mask = brick_mask3(xm, ym, zm);
                 bits = __ldg(g.bocc + (b[0] + (int64_t)g.nb[0] * (b[1] + (int64_t)g.nb[1] * b[QD2]))) & mask;
                 if ((Q.covered >> lane) & 1u) bits = 0;  // covered already: no more pairs
             }

@@ -385,6 +385,18 @@ __device__ __forceinline__ bool brick_reach(const Grid<D>& g, const int32_t* k, 
     return ok;
 }
 
+// Cell mask of a 4x4x4 brick (bit x + 4y + 16z) from its per-dimension spans xm, ym, zm (4 bits each): the x
+// span placed in the selected rows by one multiply (xm < 16 against bits 4 apart: no carries), then the row
+// plane copied into the selected z planes.
+__device__ __forceinline__ unsigned long long brick_mask3(uint32_t xm, uint32_t ym, uint32_t zm) {
+    const uint32_t ys = (ym & 1u) | ((ym & 2u) << 3) | ((ym & 4u) << 6) | ((ym & 8u) << 9);
+    const uint32_t plane = xm * ys;
+    const uint32_t p2 = plane | (plane << 16);
+    const uint32_t lo = p2 & (((0u - (zm & 1u)) & 0xFFFFu) | ((0u - ((zm >> 1) & 1u)) & 0xFFFF0000u));
+    const uint32_t hi = p2 & (((0u - ((zm >> 2) & 1u)) & 0xFFFFu) | ((0u - ((zm >> 3) & 1u)) & 0xFFFF0000u));
+    return ((unsigned long long)hi << 32) | lo;
+}
+
 // bits of cells [lo, hi] within brick b of a side of 2^SB cells
 template <int SB>
 __device__ __forceinline__ uint32_t brick_span(int32_t lo, int32_t hi, int32_t b) {
@@ -417,16 +429,14 @@ __device__ __forceinline__ bool visit_bricks(const Grid<D>& g, const int32_t* k,
             for (int32_t ax = lo[0] >> SB; ax <= (hi[0] >> SB); ax++) {
                 const int32_t bx = brick_at<OWN_FIRST>(lo[0] >> SB, k[0] >> SB, ax);
                 const uint32_t xm = brick_span<SB>(lo[0], hi[0], bx);
-                unsigned long long row = 0;
-#pragma unroll
-                for (int y = 0; y < SIDE; y++)
-                    if ((ym >> y) & 1u) row |= (unsigned long long)xm << (SIDE * y);
-                unsigned long long mask = row;
-                if (D == 3) {
+                unsigned long long mask;
+                if constexpr (D == 3) {
+                    mask = brick_mask3(xm, ym, zm);
+                } else {
                     mask = 0;
 #pragma unroll
-                    for (int z = 0; z < SIDE; z++)
-                        if ((zm >> z) & 1u) mask |= row << (SIDE * SIDE * z);
+                    for (int y = 0; y < SIDE; y++)
+                        if ((ym >> y) & 1u) mask |= (unsigned long long)xm << (SIDE * y);
                 }
                 const int64_t word = bx + (int64_t)g.nb[0] * (by + (D == 3 ? (int64_t)g.nb[1] * bz : 0));
                 unsigned long long bits = __ldg(g.bocc + word) & mask;
