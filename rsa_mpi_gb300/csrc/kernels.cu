@@ -423,6 +423,15 @@ __global__ void k_probe(Grid<D> g, Geo<D> geo, CandArgs c) {
     }
 }
 
+// Reach of a candidate-candidate search: the round's largest candidate radius when the host gives it, else the
+// grid's largest radius.
+__device__ __forceinline__ double cand_rmax(const Grid<D>& g, const CandArgs& c) {
+    return c.rcmaxf > 0.f ? c.rcmax : g.rmax;
+}
+__device__ __forceinline__ float cand_rmaxf(const Grid<D>& g, const CandArgs& c) {
+    return c.rcmaxf > 0.f ? c.rcmaxf : g.rmaxf;
+}
+
 // Visits the same-round candidates in the stencil around cell k (linked lists head/next).
 template <class F>
 __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c,
@@ -528,7 +537,7 @@ __device__ __forceinline__ bool collect_body(const Grid<D>& g, const Geo<D>& geo
         if constexpr (!F32) {
             int32_t k[D];
             cell_of<D>(g, geo, x, k);
-            visit_candidates(g, geo, c, k, nullptr, search_r2(r, g.rmax), [&](int32_t j, const double* img) {
+            visit_candidates(g, geo, c, k, nullptr, search_r2(r, cand_rmax(g, c)), [&](int32_t j, const double* img) {
                 if (!precedes(c.key[j], j, key, i)) return false;
                 if (collide64<D>(r, x, c.rad[j], img)) record(j);
                 return false;
@@ -543,7 +552,7 @@ __device__ __forceinline__ bool collect_body(const Grid<D>& g, const Geo<D>& geo
             }
             float rf = __double2float_rn(r);
         asm volatile("" : "+f"(rf));  // not rematerialised in the loop below: the conversion runs on the FP64 pipe
-            visit_candidates_o(g, c, k, offq, search_r2f(rf, g.rmaxf), [&](int32_t j, const int32_t* o, const int8_t* q) {
+            visit_candidates_o(g, c, k, offq, search_r2f(rf, cand_rmaxf(g, c)), [&](int32_t j, const int32_t* o, const int8_t* q) {
                 if (!precedes(c.key[j], j, key, i)) return false;
                 if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) record(j);
                 return false;
@@ -599,7 +608,7 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
                     if constexpr (!F32) {
                         int32_t k[D];
                         cell_of<D>(g, geo, x, k);
-                        visit_candidates(g, geo, c, k, nullptr, search_r2(r, g.rmax), [&](int32_t j, const double* img) {
+                        visit_candidates(g, geo, c, k, nullptr, search_r2(r, cand_rmax(g, c)), [&](int32_t j, const double* img) {
                             if (!precedes(c.key[j], j, key, i)) return false;
                             if (collide64<D>(r, x, c.rad[j], img)) judge(j);
                             return any_acc;
@@ -614,7 +623,7 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
                         }
                         float rf = __double2float_rn(r);
         asm volatile("" : "+f"(rf));  // not rematerialised in the loop below: the conversion runs on the FP64 pipe
-                        visit_candidates_o(g, c, k, offq, search_r2f(rf, g.rmaxf), [&](int32_t j, const int32_t* o, const int8_t* q) {
+                        visit_candidates_o(g, c, k, offq, search_r2f(rf, cand_rmaxf(g, c)), [&](int32_t j, const int32_t* o, const int8_t* q) {
                             if (!precedes(c.key[j], j, key, i)) return false;
                             if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) judge(j);
                             return any_acc;

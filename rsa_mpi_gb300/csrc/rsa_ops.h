@@ -58,6 +58,10 @@ struct CandArgs {
     uint8_t* nblk;
     uint32_t* und;      // undecided count after each settle iteration (und[0] after collect)
     uint64_t* gather;   // keys of accepted candidates (count cap)
+    // the largest candidate radius of the round (0: the grid's rmax): it bounds the candidate-candidate search
+    // of collect and settle, which otherwise reaches for the grid's largest placed radius
+    double rcmax;
+    float rcmaxf;
     // lazy candidates (FP32-form darts): until the probe forms the exact position, cell holds the dart's
     // voxel and pos its 53 random bits per coordinate; lvox and llen are that round's voxel list and length
     int32_t lazy;

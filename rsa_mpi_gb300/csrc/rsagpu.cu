@@ -132,6 +132,7 @@ struct rsagpu_algo {
     rsagpu_radgen rg;
     int nbshots = 6000;
     double rmax_algo = 0;  // m_r_max: the largest r_max of the radius generators so far
+    double cand_rmax = 0;  // the largest candidate radius of the current round (0: unknown, the grid's rmax)
     const DimOps* ops = nullptr;
     cudaStream_t stream = nullptr;
     // voxels
@@ -454,6 +455,11 @@ CandArgs cand_args(rsagpu_algo* A, uint32_t n) {
     c.lazy = A->lazy ? 1 : 0;
     c.lvox = A->vox[A->cur];
     for (int d = 0; d < A->dom->dim; d++) c.llen[d] = A->len[d];
+    // bounded by the grid's rmax, as the search was before (its stencil rows reach no further)
+    const double rg = A->dom->grid.a.rmax;
+    const double rc = A->cand_rmax > 0 && A->cand_rmax < rg ? A->cand_rmax : rg;
+    c.rcmax = rc;
+    c.rcmaxf = (float)rc;
     return c;
 }
 
@@ -983,6 +989,7 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         da.radius = A->rg.r[A->rg.idx];
         set_dart_radius_law(A->rg, &da);
         da.phase = A->rg.phase[A->rg.idx];
+        A->cand_rmax = A->rg.uniform ? A->rg.u_rmax : da.radius;  // every dart of the round has this radius or less
         const auto tp0 = std::chrono::steady_clock::now();
         ev_record(A, 0);
         CandArgs c = cand_args(A, (uint32_t)C);
@@ -1511,6 +1518,10 @@ int rsagpu_algo_replay_round(rsagpu_algo* algo, uint64_t n, const double* pos, c
         else CK(cudaMemsetAsync(c.phase, 0, n * sizeof(int32_t), algo->stream));
         CK(cudaMemsetAsync(c.state, ST_UNDECIDED, n, algo->stream));
         algo->lazy = false;  // exact positions given
+        double rc = 0;
+        for (uint64_t i = 0; i < n; i++) rc = std::max(rc, rad[i]);
+        algo->cand_rmax = rc;
+        c = cand_args(algo, (uint32_t)n);
         *n_new = decide_round(algo, (uint32_t)n, max_new, may_outreach != 0, true);
         std::vector<uint8_t> st(n);
         CK(cudaMemcpyAsync(st.data(), c.state, n, cudaMemcpyDeviceToHost, algo->stream));
