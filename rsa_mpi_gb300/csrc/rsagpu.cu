@@ -133,6 +133,9 @@ struct rsagpu_algo {
     int nbshots = 6000;
     double rmax_algo = 0;  // m_r_max: the largest r_max of the radius generators so far
     double cand_rmax = 0;  // the largest candidate radius of the current round (0: unknown, the grid's rmax)
+    // a learned-schedule input: the cells of a grid for the smallest radius of the generators so far
+    double feat_rmin = 0;
+    int64_t feat_ncells = 0;
     const DimOps* ops = nullptr;
     cudaStream_t stream = nullptr;
     // voxels
@@ -505,6 +508,23 @@ void regrid(rsagpu_algo* A, double rmin, double rmax) {
                                          A->h_counters[1], (unsigned long long)total);
 }
 
+// Staged grid of a generator of several radius classes (largest first): the cells are sized for the smallest
+// radius placed so far or drawn in the current class, not for the generator's smallest, so that the rounds of
+// the large classes walk few cells; the grid is rebuilt with the spheres kept (regrid) when a smaller class
+// begins.  Every decision is exact, so the cell size changes no result.
+double stage_radius(const rsagpu_radgen& rg) {
+    if (rg.uniform) return rg.u_rmin;
+    const int last = std::min<int>(rg.idx, (int)rg.r.size() - 1);
+    double r = rg.r[0];
+    for (int j = 1; j <= last; j++) r = std::min(r, rg.r[j]);
+    return r;
+}
+
+void stage_grid(rsagpu_algo* A) {
+    const double want = stage_radius(A->rg);
+    if (want < A->dom->grid.rmin) regrid(A, want, A->dom->grid.rmax);
+}
+
 void ensure_vox(rsagpu_algo* A, int which, uint64_t n) {
     const int D = A->dom->dim;
     if (n <= A->vox_cap[which]) return;
@@ -854,7 +874,10 @@ bool end_round(rsagpu_algo* A, uint64_t n_shots, uint64_t n_new, bool* refined, 
     rsagpu_radgen& rg = A->rg;
     if (rg.idx < (int)rg.n.size()) {
         rg.n[rg.idx] = rg.n[rg.idx] - n_new;
-        if (rg.n[rg.idx] == 0) rg.idx++;
+        if (rg.n[rg.idx] == 0) {
+            rg.idx++;
+            if (rg.idx < (int)rg.n.size()) stage_grid(A);
+        }
     }
     const bool done = rg.idx >= (int)rg.n.size();
     const double miss = miss_rate(n_shots, n_hits);
@@ -880,7 +903,7 @@ bool end_round(rsagpu_algo* A, uint64_t n_shots, uint64_t n_new, bool* refined, 
         f[7] = (float)(std::log2((double)A->placed + 1) / 32);
         f[8] = (float)(A->placed * ball_volume(D, r) / vol);
         f[9] = (float)D / 8;
-        f[10] = (float)(std::log2((double)A->V / (double)g.ncells + 1e-9) / 32);
+        f[10] = (float)(std::log2((double)A->V / (double)A->feat_ncells + 1e-9) / 32);
         f[11] = (float)((double)n_hits / ((double)A->V + 1));
         f[12] = (float)(std::log2((double)V0) / 32);
         f[13] = (float)(A->prev_level_start_V > 0
@@ -1335,9 +1358,13 @@ int rsagpu_algo_create(rsagpu_domain* dom, const rsagpu_radgen* rg, int nbshots,
             A->d_err = dalloc<uint32_t>(2);
             CK(cudaMemset(A->d_err, 0, 2 * sizeof(uint32_t)));
             A->d_visits = dalloc<unsigned long long>(2);
-            // the algo rebuilds the domain's grid and drops its spheres (operator_algorithm.ixx:25-26)
-            build_grid(dom, rg->rmin(), std::max(rg->rmax(), 0.0));
-            dom->grid.a.mono = rg->r.size() == 1 && !rg->uniform;
+            // the algo rebuilds the domain's grid and drops its spheres (operator_algorithm.ixx:25-26); the
+            // grid of the first class (stage_grid), which holds one radius only
+            const double rmax = std::max(rg->rmax(), 0.0);
+            A->feat_rmin = rg->rmin();
+            A->feat_ncells = plan_grid(dom->dim, dom->inf, dom->L, A->feat_rmin, rmax).a.ncells;
+            build_grid(dom, stage_radius(A->rg), rmax);
+            dom->grid.a.mono = !rg->uniform;
             dom->grid.a.rmono = rg->r.front();
             A->placed = 0;
             ensure_cand(A, 1024);
@@ -1453,11 +1480,16 @@ int rsagpu_algo_reset_radgen(rsagpu_algo* algo, const rsagpu_radgen* rg) {
         // operator_algorithm.ixx:238-250
         if (algo->rg.rmax() < rg->rmax()) raise(RSAGPU_ERR_ARG, "Incorrect maximal radius");
         set_device(algo->dom);
-        // a smaller minimal radius needs smaller cells (one centre per cell): regrid, keeping the spheres
-        if (rg->rmin() < algo->dom->grid.rmin) regrid(algo, rg->rmin(), algo->dom->grid.rmax);
         algo->rmax_algo = std::max(algo->rmax_algo, rg->rmax());
         algo->rg = *rg;
         algo->rg.idx = 0;
+        // a smaller radius needs smaller cells (one centre per cell): regrid, keeping the spheres
+        stage_grid(algo);
+        if (rg->rmin() < algo->feat_rmin) {
+            algo->feat_rmin = rg->rmin();
+            algo->feat_ncells =
+                plan_grid(algo->dom->dim, algo->dom->inf, algo->dom->L, algo->feat_rmin, algo->dom->grid.rmax).a.ncells;
+        }
         algo->begun = false;
         // spheres of the previous generator keep their radii: the grid's one-radius shortcut holds only if
         // the new generator has the same single radius
