@@ -2126,9 +2126,7 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
 void op_refine_mask(const GridArgs& ga, const RefineArgs& a, int f32, cudaStream_t s) {
     if (a.V == 0) return;
     // Level 0 (one voxel per cell, 2x2x2 blocks in the list): 8-lane groups over their box of cells.  Deeper
-    // levels: the per-lane walk.  There the siblings share one cell and walk the same rows in step, and most
-    // voxels are covered by a sphere of the first rows, where the walk stops; measured on the 3D r = 0.002
-    // workload, a shared gather per cell (or a near-rows pass with the rest compacted) was slower.
+    // levels of 3D grids with a brick map: the warp queue of (voxel, cell) pairs.  Else the per-lane walk.
     if (f32 && a.level == 0) {
         k_refine_mask32c<<<nblocks(a.V, COOP_BLOCK), COOP_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
     } else if (f32 && D == 3 && ga.bocc && ga.ncells < (1ll << 32)) {
