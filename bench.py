@@ -105,9 +105,9 @@ class ClockSampler:
 
 
 FORM_NAMES = {0: "plain FP64", 1: "FP32 screen + FP64 guard-band retest"}
-# the mask pass: one kernel per launch (FP32 form: the cooperative kernel at level 0, the per-lane walk below);
+# the mask pass: one kernel per launch (FP32 form, 3D: the cooperative kernel at level 0, the warp queue below);
 # FORM_TRAFFIC names its entry in profiles/refine_mask_traffic.json
-FORM_KERNEL = {0: "k_refine_mask", 1: "k_refine_mask32c (level 0) + k_refine_mask32"}
+FORM_KERNEL = {0: "k_refine_mask", 1: "k_refine_mask32c (level 0) + k_refine_mask32q (levels >= 1)"}
 FORM_TRAFFIC = {0: "k_refine_mask", 1: "mask_pass_fp32"}
 
 
