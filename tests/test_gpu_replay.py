@@ -53,6 +53,23 @@ def test_replay_polydisperse_exact_cap(name, form):
 
 
 @pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
+@pytest.mark.parametrize("seed", [11, 13])
+@pytest.mark.parametrize("name", ["p2d_poly_s3", "p3d_poly_small_s2"])
+def test_replay_polydisperse_other_seeds(name, seed, form):
+    """More class transitions: the GPU's grid is rebuilt for each smaller class (cells sized for the radii
+    placed so far) and the candidate searches reach the round's class radius; every decision and voxel set
+    still matches the oracle round by round."""
+    case = INDEX[name]
+    ora, algo, dom, rounds = lockstep(case, seed, cap_exact=True, form=form)
+    po, ro, fo = sort_spheres(*ora.spheres())
+    pg, rg, fg = sort_spheres(*dom.arrays())
+    np.testing.assert_array_equal(po, pg)
+    np.testing.assert_array_equal(ro, rg)
+    np.testing.assert_array_equal(fo, fg)
+    assert dom.check() == (0, 0)
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
 @pytest.mark.parametrize("name", ["r2d_r0.02x0.7_s1", "r3d_r0.05x0.8_s2"])
 def test_replay_reiteration_reproduces_reference_output(name, form):
     """reset_radius_generator with a smaller radius on the same domain, then proceed again: the grid is
