@@ -99,6 +99,29 @@ def test_replay_reiteration_reproduces_reference_output(name, form):
     assert dom.check() == (0, 0)
 
 
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
+def test_replay_reiteration_with_radius_classes(form):
+    """reset_radius_generator between two generators of two classes each: the GPU's grid is staged for each
+    class, and again at the reset for the second generator's first class; every decision and voxel set agrees
+    with the oracle, and so do the sphere sets after each proceed."""
+    case = {"dim": 2, "nbshots": 2000, "volume_mode": 0, "L": [1.0, 1.0],
+            "classes": [[0.02, 0.25, 0], [0.01, 0.1, 1]]}
+    ora, algo, dom = make_pair(case, cap_exact=True, form=form)
+    second = [(0.008, 0.04, 2), (0.004, 0.02, 3)]
+    for stage in range(2):
+        if stage:
+            ora.reset(second, volume=1.0)
+            algo.reset_radius_generator(RadiusGenerator(2, second, volume=1.0))
+        drive(ora, algo, 5 + stage)
+        po, ro, fo = sort_spheres(*ora.spheres())
+        pg, rg, fg = sort_spheres(*dom.arrays())
+        np.testing.assert_array_equal(po, pg)
+        np.testing.assert_array_equal(ro, rg)
+        np.testing.assert_array_equal(fo, fg)
+    assert set(np.unique(fg).tolist()) == {0, 1, 2, 3}
+    assert dom.check() == (0, 0)
+
+
 @pytest.mark.parametrize("name", ["t2d_r0.05_s0", "t3d_r0.05_s0"])
 def test_replayed_output_files_list_the_reference_cells_in_order(name, tmp_path):
     """The spheres of a replayed run, written with the reference's cell order: the same cell sequence as the
