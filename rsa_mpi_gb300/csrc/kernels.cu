@@ -432,7 +432,8 @@ __device__ __forceinline__ float cand_rmaxf(const Grid<D>& g, const CandArgs& c)
     return c.rcmaxf > 0.f ? c.rcmaxf : g.rmaxf;
 }
 
-// Visits the same-round candidates in the stencil around cell k (linked lists head/next).
+// Visits the same-round candidates in the stencil around cell k (linked lists head/next): f(j, img, q), img the
+// image of candidate j seen through the periodic shift q (q = 0: its own position).
 template <class F>
 __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c,
                                                  const int32_t* k, const float* qo, float R2q, F&& f) {
@@ -448,7 +449,7 @@ __device__ __forceinline__ void visit_candidates(const Grid<D>& g, const Geo<D>&
 #pragma unroll
                     for (int d = 0; d < D; d++) p[d] = c.pos[(uint64_t)j * D + d];
                     image_of<D>(geo, p, q, img);
-                    if (f(j, img)) return true;
+                    if (f(j, img, q)) return true;
                 }
             }
         }
@@ -530,16 +531,18 @@ __device__ __forceinline__ bool collect_body(const Grid<D>& g, const Geo<D>& geo
         const double r = c.rad[i];
         const uint64_t key = c.key[i];
         int nb = 0;
-        auto record = [&](int32_t j) {
-            if (nb < NB) c.blk[(uint64_t)i * NB + nb] = j;
+        // a collider seen through the periodic boundary is stored with BLK_WRAP set (the count cap's pass
+        // structure treats it as the reference's ghost copy)
+        auto record = [&](int32_t j, const int8_t* q) {
+            if (nb < NB) c.blk[(uint64_t)i * NB + nb] = wrapped<D>(q) ? (int32_t)((uint32_t)j | BLK_WRAP) : j;
             nb++;
         };
         if constexpr (!F32) {
             int32_t k[D];
             cell_of<D>(g, geo, x, k);
-            visit_candidates(g, geo, c, k, nullptr, search_r2(r, cand_rmax(g, c)), [&](int32_t j, const double* img) {
+            visit_candidates(g, geo, c, k, nullptr, search_r2(r, cand_rmax(g, c)), [&](int32_t j, const double* img, const int8_t* q) {
                 if (!precedes(c.key[j], j, key, i)) return false;
-                if (collide64<D>(r, x, c.rad[j], img)) record(j);
+                if (collide64<D>(r, x, c.rad[j], img)) record(j, q);
                 return false;
             });
         } else {
@@ -554,12 +557,13 @@ __device__ __forceinline__ bool collect_body(const Grid<D>& g, const Geo<D>& geo
         asm volatile("" : "+f"(rf));  // not rematerialised in the loop below: the conversion runs on the FP64 pipe
             visit_candidates_o(g, c, k, offq, search_r2f(rf, cand_rmaxf(g, c)), [&](int32_t j, const int32_t* o, const int8_t* q) {
                 if (!precedes(c.key[j], j, key, i)) return false;
-                if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) record(j);
+                if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) record(j, q);
                 return false;
             });
         }
         if (nb == 0) {
             c.state[i] = ST_ACCEPTED;
+            c.nblk[i] = 0;  // read again by the count cap's passes
             return false;
         }
         c.nblk[i] = nb > NB ? (uint8_t)NB_OVERFLOW : (uint8_t)nb;
@@ -598,7 +602,7 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
                     all_rej &= (s == ST_REJECTED);
                 };
                 if (nb != NB_OVERFLOW) {
-                    for (int b = 0; b < nb; b++) judge(c.blk[(uint64_t)i * NB + b]);
+                    for (int b = 0; b < nb; b++) judge(blk_index(c.blk[(uint64_t)i * NB + b]));
                 } else {
                     double x[D];
 #pragma unroll
@@ -608,7 +612,7 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
                     if constexpr (!F32) {
                         int32_t k[D];
                         cell_of<D>(g, geo, x, k);
-                        visit_candidates(g, geo, c, k, nullptr, search_r2(r, cand_rmax(g, c)), [&](int32_t j, const double* img) {
+                        visit_candidates(g, geo, c, k, nullptr, search_r2(r, cand_rmax(g, c)), [&](int32_t j, const double* img, const int8_t*) {
                             if (!precedes(c.key[j], j, key, i)) return false;
                             if (collide64<D>(r, x, c.rad[j], img)) judge(j);
                             return any_acc;
@@ -685,6 +689,176 @@ __global__ void k_cut_accepted(CandArgs c, int use_pivot, double pivot, uint64_t
     const uint64_t key = c.key[i];
     const bool drop = use_pivot ? ((double)(key >> 32) > pivot) : (key > key_cut);
     if (drop) c.state[i] = ST_REJECTED;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Count cap under the reference rule: the pass structure of add_to_sample (operator_algorithm.ixx:383-443)
+// over find_solve_conflicts (operator_cells_and_data_storage.ixx:79-143).  A pass classifies its candidates
+// in key order.  A candidate is Conflict when a preceding colliding candidate of the pass is seen through the
+// periodic boundary (the reference's ghost copy, which stays Undecided during a pass) or is itself Conflict;
+// else Skip when one is Undecided; else Undecided.  Where a candidate has colliders of both kinds the
+// reference takes the first in its cell-scan order; here Conflict wins.  Each classification depends only on
+// preceding candidates, so it is a monotone fixpoint like settle: the smallest unclassified key always
+// classifies.  The host then compares the pass's Undecided count with the cap (retain_only_first_elements
+// with the pivot, or validation and the next pass of the Conflict ones).
+// ------------------------------------------------------------------------------------------------
+// Visits the preceding colliders of alive candidate i, stored by collect or, after an overflow, walked again:
+// f(j, wrapped) returns true to stop.
+template <bool F32, class F>
+__device__ __forceinline__ void visit_colliders(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, uint32_t i,
+                                                uint32_t& rt, F&& f) {
+    const uint8_t nb = c.nblk[i];
+    if (nb != NB_OVERFLOW) {
+        for (int b = 0; b < nb; b++) {
+            const int32_t e = c.blk[(uint64_t)i * NB + b];
+            if (f(blk_index(e), blk_wrapped(e))) return;
+        }
+        return;
+    }
+    double x[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)i * D + d];
+    const double r = c.rad[i];
+    const uint64_t key = c.key[i];
+    if constexpr (!F32) {
+        int32_t k[D];
+        cell_of<D>(g, geo, x, k);
+        visit_candidates(g, geo, c, k, nullptr, search_r2(r, cand_rmax(g, c)), [&](int32_t j, const double* img, const int8_t* q) {
+            if (!precedes(c.key[j], j, key, i)) return false;
+            return collide64<D>(r, x, c.rad[j], img) && f(j, wrapped<D>(q));
+        });
+    } else {
+        int32_t k[D];
+        float offq[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            k[d] = c.kc[(uint64_t)i * D + d];
+            offq[d] = c.off[(uint64_t)i * D + d];
+        }
+        float rf = __double2float_rn(r);
+        asm volatile("" : "+f"(rf));
+        visit_candidates_o(g, c, k, offq, search_r2f(rf, cand_rmaxf(g, c)), [&](int32_t j, const int32_t* o, const int8_t* q) {
+            if (!precedes(c.key[j], j, key, i)) return false;
+            return cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt) && f(j, wrapped<D>(q));
+        });
+    }
+}
+
+// the candidates of the first pass: every alive candidate (the greedy settle's states are replaced)
+__global__ void k_pass_begin(CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    const bool in = t < nalive;
+    if (in) c.state[c.alive[t]] = ST_UNDECIDED;
+    const uint32_t mask = __ballot_sync(0xffffffffu, in);
+    if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[0], (uint32_t)__popc(mask));
+}
+
+// One classification step of alive candidate i of the pass; returns true when it is still unclassified.
+template <bool F32>
+__device__ __forceinline__ bool pass_body(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, uint32_t i,
+                                          uint32_t& rt) {
+    if (load_state(c.state, i) != ST_UNDECIDED) return false;
+    bool conflict = false, any_u = false, pending = false;
+    visit_colliders<F32>(g, geo, c, i, rt, [&](int32_t j, bool wrap) {
+        const uint8_t s = load_state(c.state, j);
+        if (s == ST_UNDECIDED || s >= ST_PASS_U) {  // j belongs to this pass
+            if (wrap || s == ST_PASS_C) conflict = true;
+            else if (s == ST_PASS_U) any_u = true;
+            else if (s == ST_UNDECIDED) pending = true;
+        }
+        return conflict;
+    });
+    if (conflict) c.state[i] = ST_PASS_C;
+    else if (pending) return true;
+    else c.state[i] = any_u ? ST_PASS_S : ST_PASS_U;
+    return false;
+}
+
+template <bool F32>
+__global__ void k_pass_step(Grid<D> g, Geo<D> geo, CandArgs c, int it) {
+    if (c.und[it - 1] == 0) return;
+    const uint32_t nalive = c.counters[0];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t rounds = (nalive + stride - 1) / stride;  // same trip count for every lane
+    uint32_t rt = 0;
+    for (uint32_t rr = 0; rr < rounds; rr++) {
+        const uint32_t t = t0 + rr * stride;
+        const bool still = t < nalive && pass_body<F32>(g, geo, c, c.alive[t], rt);
+        const uint32_t mask = __ballot_sync(0xffffffffu, still);
+        if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[it], (uint32_t)__popc(mask));
+    }
+    if (F32) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rt += __shfl_xor_sync(0xffffffffu, rt, o);
+        if ((threadIdx.x & 31) == 0 && rt) atomicAdd(&c.counters[4], rt);
+    }
+}
+
+// keys of the pass's Undecided candidates (counters[3] = their number)
+__global__ void k_pass_gather(CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    bool u = false;
+    uint32_t i = 0;
+    if (t < nalive) {
+        i = c.alive[t];
+        u = c.state[i] == ST_PASS_U;
+    }
+    const uint32_t slot = warp_append(&c.counters[3], u);
+    if (u) c.gather[slot] = c.key[i];
+}
+
+// End of a pass.  PASS_VALIDATE: Undecided -> accepted, Skip -> rejected, Conflict kept for the next pass
+// (update_sphere_tags).  PASS_PIVOT: Undecided with priority <= pivot -> accepted, every other candidate not
+// accepted -> rejected (retain_only_first_elements).  PASS_END: every candidate not accepted -> rejected.
+constexpr int PASS_VALIDATE = CAP_PASS_VALIDATE, PASS_PIVOT = CAP_PASS_PIVOT;
+__global__ void k_pass_close(CandArgs c, int mode, double pivot) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    if (t >= nalive) return;
+    const uint32_t i = c.alive[t];
+    const uint8_t s = c.state[i];
+    if (s == ST_ACCEPTED) return;
+    uint8_t ns = ST_REJECTED;
+    if (mode == PASS_VALIDATE) {
+        if (s == ST_PASS_U) ns = ST_ACCEPTED;
+        else if (s == ST_PASS_C) ns = ST_PASS_C;
+    } else if (mode == PASS_PIVOT) {
+        if (s == ST_PASS_U && !((double)(c.key[i] >> 32) > pivot)) ns = ST_ACCEPTED;
+    }
+    if (ns != s) c.state[i] = ns;
+}
+
+// The next pass: the Conflict candidates that collide with no candidate validated so far.  A validated
+// candidate that collides with a Conflict one always precedes it (a later one would have seen the Conflict
+// candidate, or its ghost copy, and been Conflict itself), so the preceding colliders are enough.
+template <bool F32>
+__global__ void k_pass_next(Grid<D> g, Geo<D> geo, CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    bool in = false;
+    uint32_t rt = 0;
+    if (t < nalive) {
+        const uint32_t i = c.alive[t];
+        if (c.state[i] == ST_PASS_C) {
+            bool hit = false;
+            visit_colliders<F32>(g, geo, c, i, rt, [&](int32_t j, bool) {
+                hit |= c.state[j] == ST_ACCEPTED;
+                return hit;
+            });
+            c.state[i] = hit ? ST_REJECTED : ST_UNDECIDED;
+            in = !hit;
+        }
+    }
+    const uint32_t mask = __ballot_sync(0xffffffffu, in);
+    if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[0], (uint32_t)__popc(mask));
+    if (F32) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rt += __shfl_xor_sync(0xffffffffu, rt, o);
+        if ((threadIdx.x & 31) == 0 && rt) atomicAdd(&c.counters[4], rt);
+    }
 }
 
 // commit: accepted candidates become placed spheres; the candidate lists are cleared.
@@ -2087,6 +2261,39 @@ void op_cut_accepted(const CandArgs& c, int use_pivot, double pivot, uint64_t ke
     count_launch();
 }
 
+void op_pass_begin(const CandArgs& c, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_pass_begin<<<nblocks(c.n, 256), 256, 0, s>>>(c);
+    count_launch();
+}
+
+void op_pass_step(const GridArgs& ga, const CandArgs& c, int it, int f32, cudaStream_t s) {
+    if (c.n == 0) return;
+    const unsigned nb = nblocks(c.n, 256) < 152u * 8u ? nblocks(c.n, 256) : 152u * 8u;
+    if (f32) k_pass_step<true><<<nb, 256, 0, s>>>(make_grid(ga), make_geo(ga), c, it);
+    else k_pass_step<false><<<nb, 256, 0, s>>>(make_grid(ga), make_geo(ga), c, it);
+    count_launch();
+}
+
+void op_pass_gather(const CandArgs& c, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_pass_gather<<<nblocks(c.n, 256), 256, 0, s>>>(c);
+    count_launch();
+}
+
+void op_pass_close(const CandArgs& c, int mode, double pivot, cudaStream_t s) {
+    if (c.n == 0) return;
+    k_pass_close<<<nblocks(c.n, 256), 256, 0, s>>>(c, mode, pivot);
+    count_launch();
+}
+
+void op_pass_next(const GridArgs& ga, const CandArgs& c, int f32, cudaStream_t s) {
+    if (c.n == 0) return;
+    if (f32) k_pass_next<true><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    else k_pass_next<false><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    count_launch();
+}
+
 void op_commit(const GridArgs& ga, const CandArgs& c, cudaStream_t s) {
     if (c.n == 0) return;
     k_commit<<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
@@ -2204,6 +2411,11 @@ const DimOps kOps = {
     op_b_refine_offsets,
     op_b_refine_write,
     op_b_results,
+    op_pass_begin,
+    op_pass_step,
+    op_pass_gather,
+    op_pass_close,
+    op_pass_next,
 };
 
 }  // namespace

@@ -32,6 +32,24 @@ enum : uint32_t {
 
 constexpr int NB = 24;     // stored lower-priority colliders per candidate (more: rescan)
 constexpr int NB_OVERFLOW = 255;
+// a stored collider seen through the periodic boundary (candidate indices stay below 2^31)
+constexpr uint32_t BLK_WRAP = 0x80000000u;
+
+__host__ __device__ __forceinline__ int32_t blk_index(int32_t e) { return (int32_t)((uint32_t)e & ~BLK_WRAP); }
+__host__ __device__ __forceinline__ bool blk_wrapped(int32_t e) { return ((uint32_t)e & BLK_WRAP) != 0; }
+
+// image shift q of a stencil walk: the neighbour is seen through the periodic boundary
+template <int D>
+__device__ __forceinline__ bool wrapped(const int8_t* q) {
+    bool w = false;
+#pragma unroll
+    for (int d = 0; d < D; d++) w |= q[d] != 0;
+    return w;
+}
+
+// count-cap passes (find_solve_conflicts with the Undecided / Conflict / Skip tags of one pass): states of the
+// candidates of the current pass next to ST_UNDECIDED (in the pass, not classified yet)
+enum : uint8_t { ST_PASS_U = 4, ST_PASS_C = 5, ST_PASS_S = 6 };
 
 template <int D>
 struct Geo {

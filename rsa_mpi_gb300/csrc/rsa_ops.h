@@ -207,7 +207,18 @@ struct DimOps {
     void (*b_refine_offsets)(const BatchArgs& b, const RefineArgs& a, uint64_t* new_off, cudaStream_t s);
     void (*b_refine_write)(const BatchArgs& b, const RefineArgs& a, cudaStream_t s);
     void (*b_results)(const BatchArgs& b, unsigned long long* counts, unsigned long long* sums, cudaStream_t s);
+    // count cap under the reference rule (the pass structure of find_solve_conflicts): the first pass's
+    // candidates, one classification step, the keys of the pass's Undecided candidates (counters[3]), the end
+    // of a pass (mode PASS_VALIDATE / PASS_PIVOT / PASS_END), and the next pass's candidates (und[0])
+    void (*pass_begin)(const CandArgs& c, cudaStream_t s);
+    void (*pass_step)(const GridArgs& g, const CandArgs& c, int iteration, int f32, cudaStream_t s);
+    void (*pass_gather)(const CandArgs& c, cudaStream_t s);
+    void (*pass_close)(const CandArgs& c, int mode, double pivot, cudaStream_t s);
+    void (*pass_next)(const GridArgs& g, const CandArgs& c, int f32, cudaStream_t s);
 };
+
+// modes of DimOps::pass_close
+constexpr int CAP_PASS_VALIDATE = 0, CAP_PASS_PIVOT = 1, CAP_PASS_END = 2;
 
 const DimOps* dim_ops(int D);
 

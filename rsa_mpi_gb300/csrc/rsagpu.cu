@@ -760,6 +760,61 @@ bool reference_pivot(int64_t n, int64_t n_first, At&& at, CountLe&& count_le, do
     return true;
 }
 
+constexpr int MAX_CAP_PASSES = 1000;
+
+// The count cap under the reference rule, on the device: the passes of add_to_sample (operator_algorithm.ixx:
+// 383-443).  Each pass classifies its candidates (DimOps::pass_step, find_solve_conflicts) and compares its
+// Undecided count with the class count given to the round; the count is passed by value, so every pass sees
+// the same one.  Above it, retain_only_first_elements (:475-519) keeps the Undecided priorities up to the pivot
+// (median_of_medians.ixx:8-157) and the round ends.  Else the pass is validated (update_sphere_tags), the round
+// ends when the count is met exactly, and the Conflict candidates that hit no validated one make the next
+// pass.  Without a collision through the periodic boundary the first pass is the greedy set.
+void reference_cap_passes(rsagpu_algo* A, const CandArgs& c, uint64_t max_new, int f32) {
+    const DimOps* ops = A->ops;
+    const GridArgs& g = A->dom->grid.a;
+    uint32_t* h = A->h_counters;
+    CK(cudaMemsetAsync(c.und, 0, (MAX_SETTLE + 1) * sizeof(uint32_t), A->stream));
+    ops->pass_begin(c, A->stream);
+    for (int pass = 0;; pass++) {
+        if (pass >= MAX_CAP_PASSES) raise(RSAGPU_ERR_NO_PROGRESS, "count cap: more than %d passes", MAX_CAP_PASSES);
+        CK(cudaMemcpyAsync(h + COUNTERS, c.und, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
+        CK(cudaStreamSynchronize(A->stream));
+        if (h[COUNTERS] == 0) break;  // no candidate left in the pass
+        int it = 1;
+        while (true) {
+            for (int b = 0; b < 4; b++, it++) {
+                if (it > MAX_SETTLE)
+                    raise(RSAGPU_ERR_NO_PROGRESS, "count-cap pass did not converge in %d iterations", MAX_SETTLE);
+                ops->pass_step(g, c, it, f32, A->stream);
+            }
+            CK(cudaMemcpyAsync(h + COUNTERS + it - 1, c.und + it - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                               A->stream));
+            CK(cudaStreamSynchronize(A->stream));
+            if (h[COUNTERS + it - 1] == 0) break;
+        }
+        CK(cudaMemsetAsync(c.counters + 3, 0, sizeof(uint32_t), A->stream));
+        ops->pass_gather(c, A->stream);
+        CK(cudaMemcpyAsync(h + 3, c.counters + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
+        CK(cudaStreamSynchronize(A->stream));
+        const uint64_t nu = h[3];
+        if (nu > max_new) {
+            DeviceSelect sel{c.gather, nu, 32, 2, A->d_sel_hist, A->stream, {}};
+            double pivot = 0;
+            if (!reference_pivot((int64_t)nu, (int64_t)max_new, [&](int64_t r) { return sel.at((uint64_t)r); },
+                                 [&](uint64_t t) { return sel.count_le(t); }, &pivot))
+                raise(RSAGPU_ERR_PIVOT, "count-cap pivot search failed (%llu undecided, cap %llu)",
+                      (unsigned long long)nu, (unsigned long long)max_new);
+            ops->pass_close(c, CAP_PASS_PIVOT, pivot, A->stream);
+            return;
+        }
+        ops->pass_close(c, CAP_PASS_VALIDATE, 0.0, A->stream);
+        if (nu == max_new) break;
+        CK(cudaMemsetAsync(c.und, 0, (MAX_SETTLE + 1) * sizeof(uint32_t), A->stream));
+        ops->pass_next(g, c, f32, A->stream);
+    }
+    ops->pass_close(c, CAP_PASS_END, 0.0, A->stream);
+}
+
 void ev_record(rsagpu_algo* A, int i) {
     if (A->timing) CK(cudaEventRecord(A->ev[i], A->stream));
 }
@@ -835,13 +890,7 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
                     ops->cut_accepted(c, 1, -1.0, 0, A->stream);
                 }
             } else {
-                DeviceSelect sel{c.gather, nacc, 32, 2, A->d_sel_hist, A->stream, {}};
-                double pivot = 0;
-                if (!reference_pivot((int64_t)nacc, (int64_t)max_new, [&](int64_t r) { return sel.at((uint64_t)r); },
-                                     [&](uint64_t t) { return sel.count_le(t); }, &pivot))
-                    raise(RSAGPU_ERR_PIVOT, "count-cap pivot search failed (%llu accepted, cap %llu)",
-                          (unsigned long long)nacc, (unsigned long long)max_new);
-                ops->cut_accepted(c, 1, pivot, 0, A->stream);
+                reference_cap_passes(A, c, max_new, f32);
             }
         }
     }
@@ -1110,6 +1159,9 @@ uint64_t count_spheres(rsagpu_domain* dom, rsagpu_algo* helper_none) {
 rsagpu_radgen* make_radgen(int dim, const double* r, const uint64_t* n, const int* ph, int k, double excl) {
     if (dim < 2 || dim > MAX_D) raise(RSAGPU_ERR_ARG, "dimension %d not supported (2..%d)", dim, MAX_D);
     if (k <= 0) raise(RSAGPU_ERR_ARG, "Empty radius generator!");
+    // the exclusion distance widens the first radius (below); a negative one could put it under the next
+    // class's radius, and the grid and the one-radius shortcut take the radii in descending order
+    if (!(excl >= 0)) raise(RSAGPU_ERR_ARG, "exclusion distance must be non-negative");
     auto* rg = new rsagpu_radgen();
     rg->dim = dim;
     std::vector<int> order(k);

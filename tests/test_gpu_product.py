@@ -81,6 +81,31 @@ def test_fp32_guard_form_matches_fp64_in_higher_dimensions_and_with_classes(dim,
     assert O.count_overlaps(dim, [0.0] * dim, L, out[1][0], out[1][1]) == 0
     if len(classes) == 1:
         assert out[1][3]["maximal"] == 1
+        # maximality re-certified by the oracle's own subdivision (all 2^D children)
+        r = classes[0][0]
+        assert O.uncovered_after_refinement(dim, [0.0] * dim, L, out[1][0], out[1][1], r, r, 40) == 0
+
+
+@pytest.mark.parametrize("dim,r", [(6, 0.3), (7, 0.4)])
+def test_six_and_seven_dimensions(dim, r):
+    """D = 6 and 7 (64 and 128 children per voxel, child masks of several words): both forms run to an empty
+    voxel list, give the same spheres, and the oracle's exact FP64 check finds no overlap."""
+    L = [1.0] * dim
+    out = []
+    for form in (_lib.RSAGPU_FORM_FP64, _lib.RSAGPU_FORM_FP32_GUARD):
+        rg = RadiusGenerator(dim, [(r, 1.0, 0)], volume=1.0)
+        dom = Domain([0.0] * dim, L, r)
+        algo = Algo(dom, rg, 6000)
+        algo.set_form(form)
+        algo.proceed(9)
+        st = algo.stats()
+        assert st["maximal"] == 1 and st["final_level"] > 0
+        pos, rad, ph = dom.arrays()
+        assert dom.check() == (0, 0)
+        out.append(pos)
+    np.testing.assert_array_equal(out[0], out[1])
+    assert len(out[0]) > 10
+    assert O.count_overlaps(dim, [0.0] * dim, L, out[1], np.full(len(out[1]), r)) == 0
 
 
 @pytest.mark.parametrize("dim,L,r0,r1,phi_ref", [
@@ -207,6 +232,69 @@ def test_replay_edge_cases():
                                np.full(3, r))
     assert list(acc) == [True, False, True]
     assert dom.check() == (0, 0)
+
+
+def _pair(form, dim, L, r):
+    """A fresh oracle and GPU sampler on the same empty periodic box (one radius, no class count)."""
+    ora = O.Oracle(dim, [0.0] * dim, list(L), [(r, 10**9, 0)], counts=True)
+    ora.begin(0)
+    rg = RadiusGenerator(dim, [(r, 10**9, 0)])
+    dom = Domain([0.0] * dim, list(L), r)
+    algo = Algo(dom, rg, 6000)
+    algo.set_form(form)
+    algo.begin()
+    return ora, dom, algo
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
+def test_reference_cap_follows_the_passes(form):
+    """A capped round under the default rule (RSAGPU_CAP_REFERENCE).  B collides with A through the
+    periodic boundary only, so in the first pass B is Conflict, and so are E1..E3, which collide with B alone.
+    The greedy set is {A, E1, E2, E3}; the reference's first pass validates only A, and the second pass (B
+    now hits A and leaves) holds E1..E3.  With a count of 2 the second pass is cut by the pivot: {A, E1, E2},
+    where a pivot over the greedy set would keep {A, E1}.  Every pass compares with the round's whole count
+    (it is passed by value), so with a bystander D and a count of 3 the round keeps 5 spheres."""
+    r = 0.05
+    pos = np.array([[0.02, 0.5], [0.97, 0.5], [0.88, 0.5], [0.97, 0.59], [0.97, 0.41]])
+    key = np.array([1, 2, 5, 6, 7], np.uint64)
+    cases = [(pos, key, 1, [1, 0, 0, 0, 0]), (pos, key, 2, [1, 0, 1, 1, 0]), (pos, key, 3, [1, 0, 1, 1, 1]),
+             (pos, key, 10, [1, 0, 1, 1, 1])]
+    pos_d = np.vstack([pos, [[0.5, 0.5]]])
+    key_d = np.array([1, 2, 5, 6, 7, 3], np.uint64)
+    cases += [(pos_d, key_d, 2, [1, 0, 0, 0, 0, 1]), (pos_d, key_d, 3, [1, 0, 1, 1, 1, 1])]
+    for p, k, mx, want in cases:
+        ora, dom, algo = _pair(form, 2, (1.0, 1.0), r)
+        n = len(k)
+        acc_o, n_o = ora.apply_round(p, k, np.full(n, r), np.zeros(n, np.int32), mx, 1)
+        acc_g, n_g = algo.replay_round(p, k << np.uint64(32), np.full(n, r), max_new=mx, may_outreach=True)
+        assert list(acc_o.astype(int)) == want, (mx, acc_o)
+        assert list(acc_g.astype(int)) == want, (mx, acc_g)
+        assert n_o == n_g == sum(want)
+        assert dom.check() == (0, 0)
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
+def test_reference_cap_matches_oracle_on_dense_periodic_batches(form):
+    """Capped rounds of random candidates in small periodic boxes (many collisions through the boundary,
+    Conflict chains, several passes), counts from 5 % to 99 % of the greedy set: the GPU keeps exactly the
+    oracle's candidates."""
+    rng = np.random.default_rng(21)
+    for dim, L, r, n in ((2, (0.3, 0.3), 0.01, 4000), (2, (0.6, 0.5), 0.01, 2500),
+                         (3, (0.25, 0.25, 0.25), 0.02, 5000), (4, (0.5, 0.5, 0.5, 0.5), 0.07, 3000)):
+        for frac in (0.05, 0.4, 0.8, 0.99):
+            pos = rng.random((n, dim)) * np.array(L)
+            key = rng.integers(0, 2**24, n).astype(np.uint64)
+            rad = np.full(n, r)
+            ph = np.zeros(n, np.int32)
+            ora, dom, algo = _pair(form, dim, L, r)
+            _, greedy = ora.apply_round(pos, key, rad, ph)  # no cap
+            mx = max(1, int(frac * greedy))
+            ora, dom, algo = _pair(form, dim, L, r)
+            acc_o, n_o = ora.apply_round(pos, key, rad, ph, mx, 1)
+            acc_g, n_g = algo.replay_round(pos, key << np.uint64(32), rad, max_new=mx, may_outreach=True)
+            assert n_o == n_g, (dim, frac, n_o, n_g)
+            assert np.array_equal(acc_o, acc_g), (dim, frac, int(np.sum(acc_o != acc_g)))
+            assert dom.check() == (0, 0)
 
 
 def test_replay_periodic_wrap():

@@ -53,6 +53,45 @@ def test_replay_polydisperse_exact_cap(name, form):
 
 
 @pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
+@pytest.mark.parametrize("name", ["p2d_poly_s3", "t3d_radius_s0"])
+def test_replay_polydisperse_reference_cap(name, form):
+    """The count-cap rule every product run uses by default (RSAGPU_CAP_REFERENCE): a capped round goes
+    through the reference's passes on the device, each pass's Undecided set compared with the class count and
+    cut by the pivot priority.  Every decision and voxel set equals the oracle's, and the final sphere set and
+    round count equal the reference's own output bit for bit."""
+    case = INDEX[name]
+    g = np.load(f"{GOLDEN}/{name}.npz")
+    ora, algo, dom, rounds = lockstep(case, case["seed"], form=form)
+    assert rounds == len(g["shots"])
+    pos, rad, ph = sort_spheres(*dom.arrays())
+    np.testing.assert_array_equal(pos, g["centers"])
+    np.testing.assert_array_equal(rad, g["radii"])
+    np.testing.assert_array_equal(ph, g["phases"])
+    assert dom.check() == (0, 0)
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
+@pytest.mark.parametrize("name,seed", [("p2d_poly_s3", s) for s in (None, 11, 12, 13, 14, 17)] +
+                         [("p3d_poly_small_s2", s) for s in (None, 12, 15)])
+def test_replay_reference_cap_against_oracle(name, seed, form):
+    """The default count-cap rule on more class transitions, against the oracle round by round (each of these
+    seeds has capped rounds where the rule keeps another set than an exact cut would).  The 3D three-class
+    case at its golden seed (2) meets a capped round in which a candidate has both a collider through the
+    periodic boundary and an ordinary one; the reference's outcome there follows its cell-scan order, so that
+    case is checked against the oracle (Conflict wins), with the reference's sphere count."""
+    case = INDEX[name]
+    ora, algo, dom, rounds = lockstep(case, case["seed"] if seed is None else seed, form=form)
+    po, ro, fo = sort_spheres(*ora.spheres())
+    pg, rg, fg = sort_spheres(*dom.arrays())
+    np.testing.assert_array_equal(po, pg)
+    np.testing.assert_array_equal(ro, rg)
+    np.testing.assert_array_equal(fo, fg)
+    assert dom.check() == (0, 0)
+    if seed is None:
+        assert len(rg) == case["n_spheres"]
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
 @pytest.mark.parametrize("seed", [11, 13])
 @pytest.mark.parametrize("name", ["p2d_poly_s3", "p3d_poly_small_s2"])
 def test_replay_polydisperse_other_seeds(name, seed, form):
@@ -66,6 +105,25 @@ def test_replay_polydisperse_other_seeds(name, seed, form):
     np.testing.assert_array_equal(po, pg)
     np.testing.assert_array_equal(ro, rg)
     np.testing.assert_array_equal(fo, fg)
+    assert dom.check() == (0, 0)
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
+@pytest.mark.parametrize("dim,r,seed", [(4, 0.12, 3), (4, 0.12, 4), (5, 0.2, 3)])
+def test_replay_higher_dimensions_against_oracle(dim, r, seed, form):
+    """D = 4 and 5, decision by decision and voxel set by voxel set against the oracle, to certified
+    maximality.  The reference's own corner table for D >= 4 (auxiliary/Path.ixx:105-114) writes out of bounds
+    and never sets dimension 0, so its subdivision keeps half of each voxel's children, each twice; the oracle
+    and the GPU list all 2^D children (bit d of the child index), and parity in D >= 4 is against the oracle."""
+    case = {"dim": dim, "nbshots": 6000, "volume_mode": 0, "L": [1.0] * dim, "classes": [[r, 1.0, 0]]}
+    ora, algo, dom, rounds = lockstep(case, seed, form=form)
+    po, ro, fo = sort_spheres(*ora.spheres())
+    pg, rg, fg = sort_spheres(*dom.arrays())
+    np.testing.assert_array_equal(po, pg)
+    np.testing.assert_array_equal(ro, rg)
+    vg, _, level = algo.voxels()
+    assert len(vg) == 0 and len(ora.voxels()[0]) == 0
+    assert level == ora.voxel_level > 0
     assert dom.check() == (0, 0)
 
 
