@@ -222,17 +222,21 @@ int rsagpu_mlp_train_step(float* master_weights, uint16_t* weights_bf16, const f
  * No counterpart in the reference.  For callers that cannot call cudaMalloc: code running inside
  * another framework's memory pool or under its allocator, a real-time loop whose device memory is
  * fixed up front, or a library that must not touch the device heap.  The caller passes device
- * buffers: d_pos (n*dim doubles, row major), d_key (n priorities, smaller first, ties broken by the
- * index), d_rad (n radii, none above r_max) and d_accepted (n bytes, written 1 for an accepted
+ * buffers: d_pos (n*dim doubles, row major, every centre within [inf, sup]), d_key (n priorities,
+ * smaller first, ties broken by the index), d_rad (n radii, none above r_max; a radius above it or a
+ * centre outside the box is found on the device and refused with RSAGPU_ERR_ARG, with d_accepted left
+ * unwritten) and d_accepted (n bytes, written 1 for an accepted
  * candidate, 0 otherwise).  The result is the same-round decision of the sampler: the sequential
  * greedy in priority order on the periodic box [inf, sup] (inf and sup are host arrays), with no
  * placed spheres.  Every temporary lives in one static device array of the library, sized for at most
  * RSAGPU_NOALLOC_MAX_CANDIDATES candidates (about 10.5 MB, held by every GPU that loads the library
  * until the process exits); larger batches are refused with RSAGPU_ERR_CAPACITY.  The first call on a
- * device looks up the array's device address with that device current (cudaGetSymbolAddress); make
+ * device looks up the array's device address with that device current (cudaGetSymbolAddress) and
+ * keeps it for the life of the process, so a cudaDeviceReset between calls is not supported; make
  * that first call before any stream capture.  Every call shares the one array and it keeps the last
  * call's contents: calls that overlap on the GPU race and give wrong results.  Work runs on `stream`
- * (a cudaStream_t, NULL = the default stream); the call returns when the output is written. */
+ * (a cudaStream_t, NULL = the default stream); the call synchronises `stream` and returns when the
+ * output is written. */
 #define RSAGPU_NOALLOC_MAX_CANDIDATES (1u << 18)
 int rsagpu_resolve_batch_noalloc(int dim, const double* inf, const double* sup, double r_max,
                                  const double* d_pos, const uint64_t* d_key, const double* d_rad,

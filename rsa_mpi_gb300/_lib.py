@@ -31,6 +31,8 @@ RSAGPU_SCHEDULE_LEARNED = 1
 RSAGPU_SCHEDULE_REFERENCE = 2
 RSAGPU_CAP_REFERENCE = 0
 RSAGPU_CAP_EXACT = 1
+RSAGPU_ERR_ARG = -1
+RSAGPU_ERR_CAPACITY = -7
 MAX_DIM = 7
 
 

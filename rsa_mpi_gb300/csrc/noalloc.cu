@@ -27,7 +27,11 @@ struct NoAllocScratch {
     uint8_t state[NA_MAX_N];
     uint8_t nblk[NA_MAX_N];
     uint32_t und[NA_MAX_IT + 1];
+    uint32_t err;  // NA_ERR_* bits of the current call
 };
+
+// input errors found on the device (the inputs live in device memory, so the host cannot check them)
+enum : uint32_t { NA_ERR_RADIUS = 1u, NA_ERR_OUTSIDE = 2u };
 
 // Device-side scratch.  In host code this name is only a host-side stand-in for the array: host code
 // reaches the device address through cudaGetSymbolAddress (see scratch_on_current_device).
@@ -35,8 +39,9 @@ static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
 template <int D>
 struct NaGeo {
-    double inf[D], L[D], inv_c[D];
+    double inf[D], sup[D], L[D], inv_c[D];
     int32_t n[D];
+    double r_max;
 };
 
 template <int D>
@@ -100,16 +105,24 @@ __global__ void k_na_clear() {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < NA_BUCKETS; i += gridDim.x * blockDim.x) S->head[i] = -1;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= (uint32_t)NA_MAX_IT; i += gridDim.x * blockDim.x)
         S->und[i] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) S->err = 0;
 }
 
 template <int D>
-__global__ void k_na_link(NaGeo<D> g, const double* pos, uint32_t n) {
+__global__ void k_na_link(NaGeo<D> g, const double* pos, const double* rad, uint32_t n) {
     NoAllocScratch* S = &g_noalloc_scratch;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double x[D];
 #pragma unroll
     for (int d = 0; d < D; d++) x[d] = pos[(uint64_t)i * D + d];
+    // the cells are sized for radii up to r_max and hold points of [inf, sup]: a larger radius or a point
+    // outside the box would miss colliders, so the call reports it instead of deciding
+    uint32_t err = rad[i] <= g.r_max ? 0u : NA_ERR_RADIUS;
+#pragma unroll
+    for (int d = 0; d < D; d++)
+        if (!(x[d] >= g.inf[d] && x[d] <= g.sup[d])) err |= NA_ERR_OUTSIDE;
+    if (err) atomicOr(&S->err, err);
     int32_t k[D];
     na_cell<D>(g, x, k);
     S->next[i] = atomicExch(S->head + na_bucket<D>(g, k), (int32_t)i);
@@ -194,7 +207,8 @@ __global__ void k_na_output(uint8_t* accepted, uint32_t n) {
 }
 
 // Device address of g_noalloc_scratch on the current device, looked up once per device with that
-// device current.
+// device current and kept for the life of the process.  A cudaDeviceReset (or any other teardown of the
+// device's primary context) makes the kept address stale, so the entry point does not support it.
 constexpr int NA_MAX_DEVICES = 64;
 std::mutex g_na_mutex;
 NoAllocScratch* g_na_ptr[NA_MAX_DEVICES] = {};
@@ -220,9 +234,27 @@ int run(const NaGeo<D>& g, const double* pos, const uint64_t* key, const double*
         cudaStream_t s, NoAllocScratch* S, const char** why) {
     const unsigned nb = (n + 255) / 256;
     k_na_clear<<<256, 256, 0, s>>>();
-    k_na_link<D><<<nb, 256, 0, s>>>(g, pos, n);
+    k_na_link<D><<<nb, 256, 0, s>>>(g, pos, rad, n);
+    count_launch(2);
+    {
+        uint32_t err = 0;
+        cudaError_t e = cudaMemcpyAsync(&err, &S->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            *why = cudaGetErrorString(e);
+            return RSAGPU_ERR_CUDA;
+        }
+        if (err & NA_ERR_RADIUS) {
+            *why = "rsagpu_resolve_batch_noalloc: a radius above r_max";
+            return RSAGPU_ERR_ARG;
+        }
+        if (err & NA_ERR_OUTSIDE) {
+            *why = "rsagpu_resolve_batch_noalloc: a centre outside [inf, sup]";
+            return RSAGPU_ERR_ARG;
+        }
+    }
     k_na_collect<D><<<nb, 256, 0, s>>>(g, pos, key, rad, n);
-    count_launch(3);
+    count_launch();
     int it = 1;
     while (true) {
         for (int b = 0; b < 4; b++, it++) {
@@ -257,8 +289,10 @@ template <int D>
 int dispatch(const double* inf, const double* sup, double r_max, const double* pos, const uint64_t* key,
              const double* rad, uint32_t n, uint8_t* accepted, cudaStream_t s, NoAllocScratch* S, const char** why) {
     NaGeo<D> g;
+    g.r_max = r_max;
     for (int d = 0; d < D; d++) {
         g.inf[d] = inf[d];
+        g.sup[d] = sup[d];
         g.L[d] = sup[d] - inf[d];
         int32_t c = (int32_t)(g.L[d] / (2 * r_max));
         if (c < 1) c = 1;

@@ -38,6 +38,14 @@ def test_errors_are_reported_without_a_gpu_call():
     assert "dimension" in L.rsagpu_last_error().decode()
     rc = L.rsagpu_radgen_create_counts(2, None, None, None, 0, 0.0, C.byref(h))
     assert rc == -1
+    # a negative exclusion distance could put the first radius under the next class's
+    r = np.array([0.02, 0.01])
+    n = np.array([10, 10], np.uint64)
+    rc = L.rsagpu_radgen_create_counts(2, _lib.ptr(r, _lib._d), _lib.ptr(n, _lib._u64), None, 2, -0.03, C.byref(h))
+    assert rc == -1 and "exclusion" in L.rsagpu_last_error().decode()
+    rc = L.rsagpu_radgen_create_counts(2, _lib.ptr(r, _lib._d), _lib.ptr(n, _lib._u64), None, 2, 0.001, C.byref(h))
+    assert rc == 0
+    assert L.rsagpu_radgen_destroy(h) == 0
 
 
 def test_python_module_mirrors_reference_names():

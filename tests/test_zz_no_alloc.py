@@ -36,6 +36,13 @@ def _allocating_path(pos, key, rad, dim, L, r):
 
 
 def _noalloc(pos, key, rad, dim, L, r):
+    rc, acc = _noalloc_call(pos, key, rad, dim, L, r)
+    _lib.check(rc)
+    return acc
+
+
+def _noalloc_call(pos, key, rad, dim, L, r):
+    """(status, decisions) of one call; the decisions buffer starts at 7 in every byte."""
     import torch
     dev = torch.device("cuda:0")
     d_pos = torch.from_numpy(pos).to(dev)
@@ -49,8 +56,7 @@ def _noalloc(pos, key, rad, dim, L, r):
                                                  C.c_void_p(d_pos.data_ptr()), C.c_void_p(d_key.data_ptr()),
                                                  C.c_void_p(d_rad.data_ptr()), len(key),
                                                  C.c_void_p(d_acc.data_ptr()), None)
-    _lib.check(rc)
-    return d_acc.cpu().numpy().astype(bool)
+    return rc, d_acc.cpu().numpy()
 
 
 @pytest.mark.parametrize("dim,L,r", [(2, [1.0, 1.0], 0.004), (3, [1.0, 0.7, 0.5], 0.02)])
@@ -60,9 +66,30 @@ def test_noalloc_matches_allocating_path_on_two_calls(dim, L, r):
         n = 200000 if call == 0 else 90000  # the second call is smaller: stale scratch must not leak in
         pos, key, rad = _batch(rng, n, dim, L, r)
         expect = _allocating_path(pos, key, rad, dim, L, r)
-        got = _noalloc(pos, key, rad, dim, L, r)
+        got = _noalloc(pos, key, rad, dim, L, r).astype(bool)
         assert got.sum() > 0
         np.testing.assert_array_equal(got, expect)
+
+
+def test_noalloc_refuses_radii_above_r_max_and_centres_outside_the_box():
+    """The cells are sized from r_max and the box: a larger radius or an outside centre would miss colliders.
+    The inputs are in device memory, so the kernel checks them and the call returns RSAGPU_ERR_ARG without
+    writing a decision; the next valid call is unaffected."""
+    rng = np.random.default_rng(77)
+    dim, L, r = 2, [1.0, 1.0], 0.01
+    pos, key, rad = _batch(rng, 5000, dim, L, r)
+    big = rad.copy()
+    big[1234] = np.nextafter(r, 1.0)
+    rc, acc = _noalloc_call(pos, key, big, dim, L, r)
+    assert rc == _lib.RSAGPU_ERR_ARG and np.all(acc == 7)
+    assert "r_max" in _lib.lib().rsagpu_last_error().decode()
+    out = pos.copy()
+    out[4321, 1] = 1.25
+    rc, acc = _noalloc_call(out, key, rad, dim, L, r)
+    assert rc == _lib.RSAGPU_ERR_ARG and np.all(acc == 7)
+    assert "outside" in _lib.lib().rsagpu_last_error().decode()
+    got = _noalloc(pos, key, rad, dim, L, r).astype(bool)
+    np.testing.assert_array_equal(got, _allocating_path(pos, key, rad, dim, L, r))
 
 
 def test_noalloc_refuses_batches_above_its_limit():
