@@ -9,6 +9,7 @@
 
 #include <array>
 #include <cstdint>
+#include <iostream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -59,7 +60,25 @@ public:
         detail::check(rsagpu_domain_spheres_volume(ptr_.get(), &v));
         return v;
     }
-    void domain_log() const {}
+    // domain_log (rsa_domain.ixx:151-162) as the reference prints it on one MPI rank: rank 0, the box, and
+    // one send and one receive ghost buffer per neighbour direction of the periodic box (3^DIM - 1 each)
+    void domain_log() const {
+        int nbuf = 1;
+        for (int d = 0; d < DIM; d++) nbuf *= 3;
+        nbuf -= 1;
+        auto write = [](const Point<DIM>& v) {
+            for (int d = 0; d < DIM; d++) std::cout << (d ? "," : "") << v[d];
+            std::cout << std::endl;
+        };
+        std::cout << " ==== log: domain [ 0 ] ==== " << std::endl;
+        std::cout << " == m_inf : ";
+        write(inf_);
+        std::cout << " == m_sup : ";
+        write(sup_);
+        std::cout << " == sbuffer size :  " << nbuf << std::endl;
+        std::cout << " == rbuffer size :  " << nbuf << std::endl;
+        std::cout << " ================================== " << std::endl;
+    }
     // extract_spheres (rsa_grid.ixx:88-98): the spheres in the reference's Real-cell order
     std::vector<rsa_sphere<DIM>> extract_spheres() const {
         std::vector<double> c, r;

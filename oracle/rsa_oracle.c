@@ -599,18 +599,19 @@ static void vox_build(rsa_oracle* o, double max_diagonal) {
 
 /* is_in_sphere (list_of_voxels.ixx:225-238): every corner within (r_s + r_min) */
 static int vox_corners_in(int D, const double* len, const double* delta, double rs, double rmin) {
+    /* Corner i's squared distance is the rounded sum, in dimension order, of (c_d - delta_d)^2 with c_d = 0
+     * or len_d.  Round-to-nearest addition is monotone, so the largest of the 2^D corner sums is the rounded
+     * sum of the per-dimension larger squares: one sum decides every corner, bit for bit. */
     const double R = rs + rmin;
     const double R2 = R * R;
-    for (int i = 0; i < (1 << D); i++) {
-        double dist2 = 0.;
-        for (int d = 0; d < D; d++) {
-            const double corner = (double)ora_corner(D, i, d) * len[d];
-            const double t = corner - delta[d];
-            dist2 += t * t;
-        }
-        if (dist2 > R2) return 0;
+    double dist2 = 0.;
+    for (int d = 0; d < D; d++) {
+        const double t0 = 0.0 - delta[d];
+        const double t1 = len[d] - delta[d];
+        const double s0 = t0 * t0, s1 = t1 * t1;
+        dist2 += s0 > s1 ? s0 : s1;
     }
-    return 1;
+    return !(dist2 > R2);
 }
 
 typedef struct {

@@ -14,6 +14,7 @@ int main() {
     user_interface::RadiusGenerator<DIM> rg(classes, domain.get_total_volume(), 0.);
     user_interface::rsa_algo<DIM> algo(domain, rg, 6000);
     algo.proceed(0);
+    domain.domain_log();
     auto spheres = domain.extract_spheres();
     double vol = domain.compute_total_volume_of_spheres();
     std::printf("spheres %zu fraction %.4f\n", spheres.size(), vol / domain.get_total_volume());

@@ -31,6 +31,9 @@ def test_facade_runs_reference_scenario(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300, cwd=tmp_path)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "spheres" in r.stdout
+    # domain_log as the reference prints it on one rank (rsa_domain.ixx:151-162)
+    log = " ==== log: domain [ 0 ] ==== \n == m_inf : 0,0,0\n == m_sup : 3.5,3.5,3.5\n == sbuffer size :  26\n"
+    assert log in r.stdout, r.stdout
     vtp = tmp_path / "ParaviewOutput" / "rsa_mpi_0" / "rsa_mpi_0_0.vtp"
     assert (tmp_path / "ParaviewOutput" / "rsa_mpi_0.pvtp").exists() and vtp.exists()
     n = int(vtp.read_text().split('NumberOfPoints="')[1].split('"')[0])
