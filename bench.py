@@ -1,7 +1,8 @@
 """Benchmark: spheres/s to certified maximality on one GB300 (and N replicas for N GPUs).
 
 Workload (one step): the 3D periodic unit cube, monodisperse r = 0.002, seed 1, sampled to certified
-maximality (no uncovered voxel left) by the plain FP64 GPU form -- about 11.5 M spheres.  Inputs are
+maximality (no uncovered voxel left) by the FP32 guard-band GPU form (--form 1, the default; --form 0 is the
+plain FP64 form, whose output is the same sphere for sphere) -- about 11.5 M spheres.  Inputs are
 the configuration only; the working set (sphere grid 434^3 cells, voxel lists of 10^8+ entries) is far
 larger than L2, so no flush is needed between steps.
 
@@ -28,6 +29,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -62,10 +64,10 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        fd, self.path = tempfile.mkstemp(prefix="rsa_bench_clocks_", suffix=".csv")
+        os.close(fd)
 
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
@@ -99,6 +101,10 @@ class ClockSampler:
                         reasons.add(n)
             except (ValueError, IndexError):
                 continue
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
@@ -122,8 +128,9 @@ def aggregate(times, counts, dist=None, device="cpu"):
     return t.tolist(), c.tolist()
 
 
-def run_gpu_step(dim, L, r, seed, form=1):
-    from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator
+def run_gpu_step(dim, L, r, seed, form=1, checksum=False):
+    """One run to maximality: (spheres, stats, mask-pass ms / bytes / voxels per launch[, centre checksum])."""
+    from rsa_mpi_gb300.sampler import Algo, Domain, RadiusGenerator, sphere_checksum
     rg = RadiusGenerator(dim, [(r, 1.0, 0)], volume=float(math.prod(L)))
     dom = Domain([0.0] * dim, L, r)
     algo = Algo(dom, rg, 6000)
@@ -132,9 +139,12 @@ def run_gpu_step(dim, L, r, seed, form=1):
     st = algo.stats()
     ms, by, vx = algo.kernel_profile()
     n = dom.count()
+    out = (n, st, ms, by, vx)
+    if checksum:
+        out += (sphere_checksum(dom.arrays()[0]),)
     algo.close()
     dom.close()
-    return n, st, ms, by, vx
+    return out
 
 
 def pinned_outputs(dim, cap):
@@ -227,13 +237,18 @@ def run_single_instances(inst, form):
     return n, ms * 1e-3
 
 
-def batched_form():
-    """Config 4 through rsagpu_batch_run, and a 64-instance sample of it run both ways and in both forms."""
-    from rsa_mpi_gb300.sampler import batch_run
+def batched_form(rank=0, world=1, dist=None):
+    """Config 4 through rsagpu_batch_run, and a 64-instance sample of it run both ways and in both forms.
+    With N ranks the 4,096 instances are split over them by partition_instances (balanced by expected sphere
+    count, no exchange); each rank runs its shard, and the spheres are summed and the seconds max-reduced."""
+    from rsa_mpi_gb300.sampler import batch_run, partition_instances
     inst = config4_instances()
-    res = batch_run(inst, form=1)
-    total = int(res["counts"].sum())
+    parts = partition_instances(inst, world)
+    res = batch_run([inst[i] for i in parts[rank]], form=1)
     st = res["stats"]
+    (seconds,), (total,) = aggregate([float(st["seconds"])], [float(res["counts"].sum())], dist,
+                                     "cuda" if dist is not None else "cpu")
+    total = int(total)
     sample = inst[::64]
     cmp = {}
     for form, name in ((0, "fp64"), (1, "fp32")):
@@ -244,7 +259,8 @@ def batched_form():
                      "same_counts": int(r2["counts"].sum()) == n1}
     base = cmp["fp64"]["spheres"] / cmp["fp64"]["single_s"]
     return {"workload": "4096 instances, half 2D / half 3D, r=0.01, log-uniform box sides, FP32 form",
-            "spheres_per_s": total / st["seconds"], "seconds": st["seconds"], "spheres": total,
+            "spheres_per_s": total / seconds, "seconds": seconds, "spheres": total,
+            "shards": world, "instances_per_shard": [len(p) for p in parts],
             "waves": st["waves"], "rounds": st["rounds"], "launches": st["launches"], "block_shapes": st["block"],
             "sample_every_64th": cmp,
             "speedup_vs_fp64": (cmp["fp32"]["spheres"] / cmp["fp32"]["batched_s"]) / base,
@@ -391,9 +407,13 @@ def main():
         primary = {"spheres_per_s": spheres / (dev_ms * 1e-3), "ms": dev_ms / args.steps, "retests": stats["retests"]}
         forms[FORM_NAMES[args.form]] = primary
         other = 1 - args.form
-        n2, st2, _, _, _ = run_gpu_step(dim, L, r, seed, other)
+        # the same spheres, by an exact centre checksum (one more run of the timed form, and the other form)
+        n1, _, _, _, _, sum1 = run_gpu_step(dim, L, r, seed, args.form, checksum=True)
+        n2, st2, _, _, _, sum2 = run_gpu_step(dim, L, r, seed, other, checksum=True)
+        primary["checksum"] = sum1
         forms[FORM_NAMES[other]] = {"spheres_per_s": n2 / (st2["ms_total"] * 1e-3), "ms": st2["ms_total"],
-                                    "retests": st2["retests"], "same_spheres": n2 == spheres // max(1, args.steps)}
+                                    "retests": st2["retests"], "checksum": sum2,
+                                    "same_spheres": n2 == n1 and sum2 == sum1}
         base = forms[FORM_NAMES[0]]["spheres_per_s"]
         for v in forms.values():
             v["speedup_vs_fp64"] = v["spheres_per_s"] / base
@@ -409,7 +429,7 @@ def main():
                                            "heuristic_spheres": h4[0], "learned_spheres": l4[0]}
         forms["learned schedule (FP32 form)"] = learned
         forms["FP32 guard band, polydisperse (config 3)"] = precision_form()
-        forms["batched (config 4)"] = batched_form()
+        forms["batched (config 4)"] = batched_form(rank, world, dist)
 
     # e2e through the C ABI, the spheres read into pinned host buffers allocated once (outside the timed region)
     e2e_n, e2e_s, d2h = 0, 0.0, 0

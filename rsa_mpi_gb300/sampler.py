@@ -278,6 +278,40 @@ def batch_run(instances, form: int = _lib.RSAGPU_FORM_FP32_GUARD, max_bytes: int
     return {"counts": counts[:n], "checksums": sums[:n], "seconds": secs[:n], "stats": stats}
 
 
+def expected_spheres(instance) -> float:
+    """The work estimate of one batched instance (dim, sup, radius, seed): its box volume over the volume of
+    one sphere, proportional to the spheres of its maximal packing."""
+    dim, sup, radius, _ = instance
+    vol = 1.0
+    for d in range(int(dim)):
+        vol *= float(sup[d])
+    return vol / _ball_volume(int(dim), float(radius))
+
+
+def _ball_volume(dim: int, r: float) -> float:
+    import math
+    return math.pi ** (dim / 2) / math.gamma(dim / 2 + 1) * r ** dim
+
+
+def partition_instances(instances, world: int):
+    """Splits independent instances over `world` ranks, balanced by expected_spheres: the largest instance
+    first to the rank with the least work so far (ties to the lower rank).  Returns one sorted index list per
+    rank; the lists are disjoint and together hold every instance.  Deterministic, so every rank computes the
+    same split with no exchange.  (The reference decomposes one domain over MPI ranks with ghost layers,
+    rsa_ghost_area / operator_ghost; independent instances need no exchange at all.)"""
+    import heapq
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    order = sorted(range(len(instances)), key=lambda i: (-expected_spheres(instances[i]), i))
+    heap = [(0.0, r) for r in range(world)]
+    parts = [[] for _ in range(world)]
+    for i in order:
+        load, r = heapq.heappop(heap)
+        parts[r].append(i)
+        heapq.heappush(heap, (load + expected_spheres(instances[i]), r))
+    return [sorted(p) for p in parts]
+
+
 def _mix64(z: np.ndarray) -> np.ndarray:
     z = z ^ (z >> np.uint64(30))
     z = z * np.uint64(0xBF58476D1CE4E5B9)
