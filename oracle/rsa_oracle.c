@@ -614,27 +614,99 @@ static int vox_corners_in(int D, const double* len, const double* delta, double 
     return !(dist2 > R2);
 }
 
-typedef struct {
-    const rsa_oracle* o;
-    const double* orig;
-    const double* len;
-    int found;
-} cover_ctx;
-
-static int cover_visit(void* vctx, uint64_t id, const double* img) {
-    cover_ctx* c = (cover_ctx*)vctx;
-    const int D = c->o->D;
-    double delta[ORA_MAX_DIM];
-    for (int d = 0; d < D; d++) delta[d] = img[d] - c->orig[d];
-    if (vox_corners_in(D, c->len, delta, c->o->st.rad[id], c->o->r_min)) {
-        c->found = 1;
-        return 1;
-    }
-    return 0;
-}
-
 static void vox_origin(const rsa_oracle* o, const int64_t* coord, const double* len, double* orig) {
     for (int d = 0; d < o->D; d++) orig[d] = o->inf[d] + (double)coord[d] * len[d];
+}
+
+/* The validated spheres by cell with one layer of ghost cells, as the reference's rsa_grid holds them
+ * (rsa_grid.ixx, ghost copies rsa_ghost_area.ixx:22-30): each cell of the padded grid lists, contiguously,
+ * the spheres of the real cell it maps to with the periodic shift of that ghost position applied.  Built
+ * once per refinement, during which the spheres do not change; the voxel passes then read the 3^D cells
+ * around a point at fixed index offsets.  The (sphere, image) pairs are those store_visit yields. */
+typedef struct {
+    int D;
+    int np[ORA_MAX_DIM];      /* padded cells per dimension (n + 2) */
+    int64_t* start;           /* padded cells + 1 */
+    uint64_t* ids;
+    double* img;              /* D doubles per entry: the image coordinates */
+    int64_t off[2187];        /* the 3^D neighbour offsets in the padded grid (3^7 at most) */
+    int noff;
+} ora_csr;
+
+static void csr_build(ora_csr* c, const ora_store* s) {
+    const int D = s->D;
+    c->D = D;
+    int64_t npc = 1;
+    for (int d = 0; d < D; d++) {
+        c->np[d] = s->n[d] + 2;
+        npc *= c->np[d];
+    }
+    c->start = (int64_t*)calloc((size_t)npc + 1, sizeof(int64_t));
+    /* counts: the real cell of each padded cell */
+    int pc[ORA_MAX_DIM] = { 0 };
+    for (int64_t p = 0; p < npc; p++) {
+        int rc[ORA_MAX_DIM];
+        for (int d = 0; d < D; d++) {
+            int k = pc[d] - 1;
+            if (k < 0) k += s->n[d];
+            else if (k >= s->n[d]) k -= s->n[d];
+            rc[d] = k;
+        }
+        int64_t cnt = 0;
+        for (int64_t i = s->head[store_cell_index(s, rc)]; i >= 0; i = s->next[i]) cnt++;
+        c->start[p + 1] = c->start[p] + cnt;
+        for (int d = 0; d < D && ++pc[d] == c->np[d]; d++) pc[d] = 0;
+    }
+    const int64_t total = c->start[npc];
+    c->ids = (uint64_t*)malloc(sizeof(uint64_t) * (total ? total : 1));
+    c->img = (double*)malloc(sizeof(double) * (total ? total : 1) * D);
+    for (int d = 0; d < D; d++) pc[d] = 0;
+    for (int64_t p = 0; p < npc; p++) {
+        int rc[ORA_MAX_DIM];
+        double sh[ORA_MAX_DIM];
+        for (int d = 0; d < D; d++) {
+            int k = pc[d] - 1;
+            sh[d] = 0.0;
+            if (k < 0) { k += s->n[d]; sh[d] = -s->L[d]; }
+            else if (k >= s->n[d]) { k -= s->n[d]; sh[d] = s->L[d]; }
+            rc[d] = k;
+        }
+        int64_t k = c->start[p];
+        for (int64_t i = s->head[store_cell_index(s, rc)]; i >= 0; i = s->next[i], k++) {
+            c->ids[k] = (uint64_t)i;
+            for (int d = 0; d < D; d++) {
+                const double x = s->pos[(size_t)i * D + d];
+                c->img[(size_t)k * D + d] = sh[d] != 0.0 ? x + sh[d] : x;
+            }
+        }
+        for (int d = 0; d < D && ++pc[d] == c->np[d]; d++) pc[d] = 0;
+    }
+    /* neighbour offsets */
+    int od[ORA_MAX_DIM] = { 0 };
+    c->noff = 0;
+    for (;;) {
+        int64_t o = 0;
+        for (int d = D - 1; d >= 0; d--) o = o * c->np[d] + (od[d] - 1);
+        c->off[c->noff++] = o;
+        int d = 0;
+        while (d < D && ++od[d] == 3) od[d++] = 0;
+        if (d == D) break;
+    }
+}
+
+static void csr_free(ora_csr* c) {
+    free(c->start);
+    free(c->ids);
+    free(c->img);
+}
+
+/* the padded cell of the point x (its real cell plus one in every dimension) */
+static int64_t csr_cell(const ora_csr* c, const ora_store* s, const double* x) {
+    int cc[ORA_MAX_DIM];
+    store_cell_coords(s, x, cc);
+    int64_t idx = 0;
+    for (int d = c->D - 1; d >= 0; d--) idx = idx * c->np[d] + (cc[d] + 1);
+    return idx;
 }
 
 /* remove_covered (list_of_voxels.ixx:30-54), including the swap-remove order. */
@@ -642,14 +714,29 @@ static void vox_remove_covered(rsa_oracle* o) {
     const int D = o->D;
     uint64_t n = o->nvox;
     uint8_t* cov = (uint8_t*)malloc(n ? n : 1);
+    ora_csr csr;
+    csr_build(&csr, &o->st);
     for (uint64_t v = 0; v < n; v++) {
         double orig[ORA_MAX_DIM], centre[ORA_MAX_DIM];
         vox_origin(o, o->vox + v * D, o->vlen, orig);
         for (int d = 0; d < D; d++) centre[d] = orig[d] + 0.5 * o->vlen[d];
-        cover_ctx c = { o, orig, o->vlen, 0 };
-        store_visit(&o->st, centre, cover_visit, &c);
-        cov[v] = (uint8_t)c.found;
+        /* is_covered (list_of_voxels.ixx:240-257): the spheres of the 3^D cells around the centre's */
+        const int64_t base = csr_cell(&csr, &o->st, centre);
+        int found = 0;
+        for (int t = 0; t < csr.noff && !found; t++) {
+            const int64_t cell = base + csr.off[t];
+            for (int64_t k = csr.start[cell]; k < csr.start[cell + 1]; k++) {
+                double delta[ORA_MAX_DIM];
+                for (int d = 0; d < D; d++) delta[d] = csr.img[(size_t)k * D + d] - orig[d];
+                if (vox_corners_in(D, o->vlen, delta, o->st.rad[csr.ids[k]], o->r_min)) {
+                    found = 1;
+                    break;
+                }
+            }
+        }
+        cov[v] = (uint8_t)found;
     }
+    csr_free(&csr);
     uint64_t size = n;
     for (int64_t v = 0; v < (int64_t)size; v++) {
         if (cov[v]) {
@@ -706,6 +793,8 @@ static void vox_subdivide(rsa_oracle* o) {
     if (!out) abort(); /* the oracle is for cases that fit in host memory */
     uint64_t k = 0;
     pre_ctx pc = { o, NULL, NULL, NULL, 0, 0 };
+    ora_csr csr;
+    csr_build(&csr, &o->st);
     for (uint64_t v = 0; v < o->nvox; v++) {
         const int64_t* pcoord = o->vox + v * D;
         double centre[ORA_MAX_DIM];
@@ -713,7 +802,14 @@ static void vox_subdivide(rsa_oracle* o) {
         for (int d = 0; d < D; d++) centre[d] = o->inf[d] + ((double)pcoord[d] + 0.5) * o->vlen[d];
         pc.centre = centre;
         pc.n = 0;
-        store_visit(&o->st, centre, pre_visit, &pc);
+        {
+            const int64_t base = csr_cell(&csr, &o->st, centre);
+            for (int t = 0; t < csr.noff; t++) {
+                const int64_t cell = base + csr.off[t];
+                for (int64_t k = csr.start[cell]; k < csr.start[cell + 1]; k++)
+                    pre_visit(&pc, csr.ids[k], csr.img + (size_t)k * D);
+            }
+        }
         for (int i = 0; i < nc; i++) {
             int64_t cc[ORA_MAX_DIM];
             double orig[ORA_MAX_DIM];
@@ -733,6 +829,7 @@ static void vox_subdivide(rsa_oracle* o) {
             }
         }
     }
+    csr_free(&csr);
     free(pc.ids);
     free(pc.imgs);
     free(o->vox);
