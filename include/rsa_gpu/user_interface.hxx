@@ -9,6 +9,7 @@
 
 #include <array>
 #include <cstdint>
+#include <functional>
 #include <iostream>
 #include <memory>
 #include <stdexcept>
@@ -164,6 +165,17 @@ public:
     static RadiusGenerator uniform(double r_min, double r_max, uint64_t nb_spheres, int phase) {
         rsagpu_radgen* g = nullptr;
         detail::check(rsagpu_radgen_create_uniform(DIM, r_min, r_max, nb_spheres, phase, &g));
+        return RadiusGenerator(std::shared_ptr<rsagpu_radgen>(g, [](rsagpu_radgen* q) { rsagpu_radgen_destroy(q); }));
+    }
+    // sac_de_billes::RadiusGenerator<DIM>(min, max, &RandomRadiusGenerator(transform, phase), nb_spheres, 0)
+    // (radius_generator.hxx:12-38) for any transform of x uniform in [0, 1): the transform is tabulated at
+    // n_knots points x = j / (n_knots - 1) and the darts interpolate it linearly
+    static RadiusGenerator random(std::function<double(double)> transform, uint64_t nb_spheres, int phase,
+                                  int n_knots = 4097) {
+        std::vector<double> t(n_knots);
+        for (int j = 0; j < n_knots; j++) t[j] = transform(j / double(n_knots - 1));
+        rsagpu_radgen* g = nullptr;
+        detail::check(rsagpu_radgen_create_table(DIM, t.data(), n_knots, nb_spheres, phase, &g));
         return RadiusGenerator(std::shared_ptr<rsagpu_radgen>(g, [](rsagpu_radgen* q) { rsagpu_radgen_destroy(q); }));
     }
     double get_max_radius() const {

@@ -85,6 +85,13 @@ int rsagpu_radgen_create_fractions(int dim, const double* radii, const double* f
  * (radius_generator.ixx:39-48, radius_generator.hxx:12-38, test/test_random_radius_generator.cpp:13-29). */
 int rsagpu_radgen_create_uniform(int dim, double r_min, double r_max, uint64_t count, int phase,
                                  rsagpu_radgen** out);
+/* Continuous radius law with any transform: knots[j] = transform(j / (n_knots - 1)), j = 0 .. n_knots - 1
+ * (2 to 2^20 positive radii); each dart's radius is the transform interpolated linearly at its x, uniform in
+ * [0, 1), kept within [min knots, max knots].  Replaces sac_de_billes::RadiusGenerator<DIM>(min_radius,
+ * max_radius, &RandomRadiusGenerator(transform, phase), nb_spheres, 0) for an arbitrary std::function
+ * transform (radius_generator.hxx:12-38, radius_generator.ixx:39-48), which the C++ facade tabulates. */
+int rsagpu_radgen_create_table(int dim, const double* knots, int n_knots, uint64_t count, int phase,
+                               rsagpu_radgen** out);
 int rsagpu_radgen_destroy(rsagpu_radgen* rg);
 int rsagpu_radgen_max_radius(const rsagpu_radgen* rg, double* out);
 int rsagpu_radgen_min_radius(const rsagpu_radgen* rg, double* out);
@@ -105,6 +112,11 @@ int rsagpu_algo_destroy(rsagpu_algo* algo);
 #define RSAGPU_SCHEDULE_LEARNED 1   /* MLP decides when to refine (heuristic as fallback) */
 #define RSAGPU_SCHEDULE_REFERENCE 2 /* the reference's round sizes: Poisson(min(nbshots, 0.01 V)) */
 int rsagpu_algo_set_form(rsagpu_algo* algo, int form, int schedule);
+/* No counterpart in the reference.  With on = 1 the FP32 form's 3D mask pass hands each surviving voxel's
+ * nearby spheres to its children, which then test those and the spheres placed since instead of walking
+ * their whole neighbourhood.  Off (the default) walks every neighbourhood.  The decisions are the same
+ * either way. */
+int rsagpu_algo_set_inherit(rsagpu_algo* algo, int on);
 /* count cap of a round that would exceed the class count */
 #define RSAGPU_CAP_REFERENCE 0    /* retain_only_first_elements pivot rule (operator_algorithm.ixx:475-519) */
 #define RSAGPU_CAP_EXACT 1        /* exactly the remaining count, smallest priorities first */
@@ -130,12 +142,14 @@ int rsagpu_algo_reset_radgen(rsagpu_algo* algo, const rsagpu_radgen* rg);
 int rsagpu_algo_trace(rsagpu_algo* algo, uint64_t* voxels, uint64_t* darts, uint64_t* accepted,
                       uint8_t* refined, int32_t* level, uint64_t cap, uint64_t* n_out);
 /* Statistics of the last proceed(): rounds, refinements, darts, settle iterations, guard-band
- * retests, device milliseconds per kernel family (darts, probe, settle, commit, refine). */
+ * retests, device milliseconds per kernel family (darts, probe, settle, commit, refine), and the count
+ * cap's passes and classification steps (reference rule). */
 typedef struct {
     uint64_t rounds, refinements, darts, accepted, settle_iterations, retests, peak_voxels;
     uint64_t bytes_darts, bytes_probe, bytes_settle, bytes_commit, bytes_refine;
     double ms_darts, ms_probe, ms_settle, ms_commit, ms_refine, ms_total;
     int32_t final_level, maximal;
+    uint64_t cap_passes, cap_steps;
 } rsagpu_stats;
 int rsagpu_algo_stats(rsagpu_algo* algo, rsagpu_stats* out);
 /* Per launch of the refinement's mask kernel in the last proceed(): device milliseconds (CUDA events

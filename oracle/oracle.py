@@ -53,6 +53,7 @@ def lib():
         L.ora_create_uniform.restype = C.c_void_p
         L.ora_create_uniform.argtypes = [C.c_int, _d, _d, C.c_double, C.c_double, C.c_uint64, C.c_int, C.c_int]
         L.ora_destroy.argtypes = [C.c_void_p]
+        L.ora_set_radius_table.argtypes = [C.c_void_p, _d, C.c_int]
         L.ora_count_from_fraction.restype = C.c_uint64
         L.ora_count_from_fraction.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double]
         L.ora_volume_sphere.restype = C.c_double
@@ -151,6 +152,16 @@ class Oracle:
                                            int(count), int(phase), int(nbshots))
         if not self._h:
             raise RuntimeError("oracle: invalid configuration")
+        return self
+
+    @classmethod
+    def table(cls, dim, inf, sup, knots, count=10**16, phase=0, nbshots=6000):
+        """A continuous radius law given by its transform's values at x = j / (len(knots) - 1), interpolated
+        linearly (an arbitrary RandomRadiusGenerator transform, radius_generator.hxx:12-38)."""
+        t = np.ascontiguousarray(knots, dtype=np.float64)
+        self = cls.uniform(dim, inf, sup, float(t.min()), float(t.max()), count, phase, nbshots)
+        if lib().ora_set_radius_table(self._h, _p(t, _d), len(t)) != 0:
+            raise RuntimeError("oracle: invalid radius table")
         return self
 
     def reset(self, classes, volume=None, exclusion=0.0):

@@ -451,6 +451,8 @@ struct rsa_oracle {
     int cap_exact;
     /* continuous radius law: radius = r_min + (r_max - r_min) x, x ~ U[0, 1) */
     int uniform_radius;
+    double* rtab; /* a tabulated transform (knots at x = j / (ntab - 1)), or NULL: r_min + (r_max - r_min) x */
+    int ntab;
     int uniform_phase;
 };
 
@@ -499,6 +501,29 @@ rsa_oracle* ora_create(int dim, const double* inf, const double* sup, double dom
  * (radius_generator.ixx:39-48, radius_generator.hxx:12-38) with transform x -> r_min + (r_max - r_min) x:
  * one entry (radius 0, nb_spheres, phase 0) in the class list, explicit r_min and r_max, every dart's
  * radius drawn after the priorities (generate_candidates, operator_algorithm.ixx:568-582). */
+/* A transform given by its values at x = j / (ntab - 1), interpolated linearly at x and kept within
+ * [r_min, r_max] (the knots' range): the tabulated form of an arbitrary RandomRadiusGenerator transform
+ * (radius_generator.hxx:12-38), with the same arithmetic as the GPU darts. */
+static double ora_table_radius(const rsa_oracle* o, double x) {
+    const double t = x * (double)(o->ntab - 1);
+    int j = (int)t;
+    if (j > o->ntab - 2) j = o->ntab - 2;
+    const double f = t - (double)j;
+    const double a = o->rtab[j], b = o->rtab[j + 1];
+    const double v = a + f * (b - a);
+    const double hi = o->r_min + (o->r_max - o->r_min);
+    return v < o->r_min ? o->r_min : (v > hi ? hi : v);
+}
+
+int ora_set_radius_table(rsa_oracle* o, const double* knots, int n) {
+    if (!o->uniform_radius || n < 2) return -1;
+    free(o->rtab);
+    o->rtab = (double*)malloc(sizeof(double) * n);
+    memcpy(o->rtab, knots, sizeof(double) * n);
+    o->ntab = n;
+    return 0;
+}
+
 rsa_oracle* ora_create_uniform(int dim, const double* inf, const double* sup, double r_min, double r_max,
     uint64_t count, int phase, int nbshots) {
     const double r0 = 0.;
@@ -557,6 +582,7 @@ void ora_destroy(rsa_oracle* o) {
     free(o->vox);
     free(o->cpos); free(o->ckey); free(o->crad); free(o->cphase);
     free(o->tr_vox); free(o->tr_shots); free(o->tr_new); free(o->tr_ref);
+    free(o->rtab);
     free(o);
 }
 
@@ -1204,7 +1230,8 @@ int ora_gen_round(rsa_oracle* o, uint64_t* n_out, uint64_t* max_new, int* may_ou
     if (o->uniform_radius) {
         /* RandomRadiusGenerator::operator() (radius_generator.hxx:27-34): law::uniform<double>(0, 1) */
         for (uint64_t i = 0; i < n; i++) {
-            o->crad[i] = o->r_min + (o->r_max - o->r_min) * ora_canonical(&o->g);
+            const double x = ora_canonical(&o->g);
+            o->crad[i] = o->rtab ? ora_table_radius(o, x) : o->r_min + (o->r_max - o->r_min) * x;
             o->cphase[i] = o->uniform_phase;
         }
     } else {

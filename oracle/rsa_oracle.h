@@ -45,6 +45,9 @@ void ora_destroy(rsa_oracle* o);
  * (RadiusGenerator with a RandomRadiusGenerator, radius_generator.ixx:39-48, radius_generator.hxx:12-38). */
 rsa_oracle* ora_create_uniform(int dim, const double* inf, const double* sup, double r_min, double r_max,
     uint64_t count, int phase, int nbshots);
+/* the uniform law's transform replaced by one tabulated at x = j / (n - 1) (the radius generator's r_min and
+ * r_max must be the knots' range) */
+int ora_set_radius_table(rsa_oracle* o, const double* knots, int n);
 
 /* rsa_algo::reset_radius_generator (operator_algorithm.ixx:238-250): new classes, same spheres; r_max stays the
  * larger one.  Returns -2 for a larger maximal radius (the reference throws). */

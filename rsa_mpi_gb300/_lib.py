@@ -49,7 +49,8 @@ class Stats(C.Structure):
                                            "retests", "peak_voxels", "bytes_darts", "bytes_probe", "bytes_settle",
                                            "bytes_commit", "bytes_refine")] + \
               [(n, C.c_double) for n in ("ms_darts", "ms_probe", "ms_settle", "ms_commit", "ms_refine", "ms_total")] + \
-              [("final_level", C.c_int32), ("maximal", C.c_int32)]
+              [("final_level", C.c_int32), ("maximal", C.c_int32)] + \
+              [(n, C.c_uint64) for n in ("cap_passes", "cap_steps")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -80,6 +81,7 @@ _SIGS = {
     "rsagpu_domain_check": (C.c_int, [_vp, _u64, _u64]),
     "rsagpu_radgen_create_counts": (C.c_int, [C.c_int, _d, _u64, _i32, C.c_int, C.c_double, C.POINTER(_vp)]),
     "rsagpu_radgen_create_uniform": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint64, C.c_int, C.POINTER(_vp)]),
+    "rsagpu_radgen_create_table": (C.c_int, [C.c_int, _d, C.c_int, C.c_uint64, C.c_int, C.POINTER(_vp)]),
     "rsagpu_radgen_create_fractions": (C.c_int, [C.c_int, _d, _d, _i32, C.c_int, C.c_double, C.c_double,
                                                  C.POINTER(_vp)]),
     "rsagpu_radgen_destroy": (C.c_int, [_vp]),
@@ -88,6 +90,7 @@ _SIGS = {
     "rsagpu_algo_create": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(_vp)]),
     "rsagpu_algo_destroy": (C.c_int, [_vp]),
     "rsagpu_algo_set_form": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "rsagpu_algo_set_inherit": (C.c_int, [_vp, C.c_int]),
     "rsagpu_algo_set_cap_rule": (C.c_int, [_vp, C.c_int]),
     "rsagpu_algo_set_schedule_params": (C.c_int, [_vp, C.c_double, C.c_uint64, C.c_uint64, C.c_double]),
     "rsagpu_algo_set_mlp": (C.c_int, [_vp, _u16, C.c_uint64]),

@@ -86,6 +86,7 @@ __host__ __device__ inline Grid<D> make_grid(const GridArgs& a) {
     g.rmono = a.rmono;
     g.rmonof = (float)a.rmono;
     g.rmaxf = (float)a.rmax;
+    g.bnew = a.bnew;
     return g;
 }
 
@@ -157,6 +158,8 @@ struct DartParams {
     int32_t phase;
     int32_t rand_radius;  // continuous radius law: radius = r_lo + r_span x (dart_radius)
     double r_lo, r_span;
+    const double* rtab;   // or a tabulated transform (ntab >= 2 knots), radii clamped to [r_lo, r_lo + r_span]
+    int32_t ntab;
     double* pos;
     uint64_t* key;
     double* rad;
@@ -185,11 +188,25 @@ struct DartParams {
 // radius of dart i: the class radius, or under a continuous law r_lo + r_span x with x the 53-bit uniform of
 // the dart's own Philox call in a separate counter space (call word 0x80000000), as the reference's transform
 // x -> r_min + (r_max - r_min) x (radius_generator.hxx:27-34)
+// With a tabulated transform T (knots T(j / (n - 1)), j = 0 .. n - 1: any law the reference's
+// RandomRadiusGenerator takes as a function of x, radius_generator.hxx:12-38) the radius is T interpolated
+// linearly at x, kept within the knots' range.
 __device__ __forceinline__ double dart_radius(const DartParams& p, uint32_t i) {
     if (!p.rand_radius) return p.radius;
     const uint4 r = philox4x32_10(make_uint4(i, p.round_lo, p.round_hi, 0x80000000u), make_uint2(p.seed_lo, p.seed_hi));
     const uint64_t bits = ((((uint64_t)r.x) << 32) | r.y) >> 11;
-    return __dadd_rn(p.r_lo, __dmul_rn(p.r_span, (double)bits * 0x1.0p-53));
+    const double x = (double)bits * 0x1.0p-53;
+    if (p.ntab >= 2) {
+        const double t = __dmul_rn(x, (double)(p.ntab - 1));
+        int32_t j = (int32_t)t;
+        j = j > p.ntab - 2 ? p.ntab - 2 : j;
+        const double f = __dsub_rn(t, (double)j);
+        const double a = p.rtab[j], b = p.rtab[j + 1];
+        const double v = __dadd_rn(a, __dmul_rn(f, __dsub_rn(b, a)));
+        const double hi = __dadd_rn(p.r_lo, p.r_span);
+        return v < p.r_lo ? p.r_lo : (v > hi ? hi : v);
+    }
+    return __dadd_rn(p.r_lo, __dmul_rn(p.r_span, x));
 }
 
 // voxel drawn by dart i (the first Philox call's words 0 and 1)
@@ -754,24 +771,133 @@ __global__ void k_pass_begin(CandArgs c) {
     if ((threadIdx.x & 31) == 0 && mask) atomicAdd(&c.und[0], (uint32_t)__popc(mask));
 }
 
-// One classification step of alive candidate i of the pass; returns true when it is still unclassified.
+// The classification.  A candidate is Conflict iff a chain of colliders of the pass, each preceding the next,
+// leads to it from a collision through the periodic boundary: Conflict never depends on the Undecided / Skip
+// outcome.  So the Conflict set is found first, as a breadth-first search: the sources are the candidates with
+// a preceding collider of the pass seen through the boundary (k_pass_sources), and each Conflict candidate marks
+// the later candidates of the pass that collide with it (k_pass_push, over the round's candidate lists).  The
+// candidates left are not Conflict, and their preceding colliders of the pass are neither Conflict nor seen
+// through the boundary, so the rest is the greedy on them (pass_body): Skip as soon as a preceding collider is
+// Undecided (the pass's accepted), Undecided once all are Skip.
+//
+// Frontiers of the search: c.gather's memory as two arrays of candidate indices, counts in counters[5 + f].
+__device__ __forceinline__ uint32_t* frontier(const CandArgs& c, int f) {
+    return reinterpret_cast<uint32_t*>(c.gather) + (uint64_t)f * c.n;
+}
+
+// Claims candidate i for the Conflict set (its state byte UNDECIDED -> ST_PASS_C, by a CAS on the word holding
+// it); true for the one thread that changed it.
+__device__ __forceinline__ bool claim_conflict(const CandArgs& c, uint32_t i) {
+    uint32_t* w = reinterpret_cast<uint32_t*>(c.state + (i & ~3u));
+    const int sh = 8 * (int)(i & 3u);
+    uint32_t old = *((volatile uint32_t*)w);
+    while (((old >> sh) & 0xffu) == ST_UNDECIDED) {
+        const uint32_t nw = (old & ~(0xffu << sh)) | ((uint32_t)ST_PASS_C << sh);
+        const uint32_t prev = atomicCAS(w, old, nw);
+        if (prev == old) return true;
+        old = prev;
+    }
+    return false;
+}
+
+template <bool F32>
+__global__ void k_pass_sources(Grid<D> g, Geo<D> geo, CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nalive = c.counters[0];
+    bool src = false;
+    uint32_t i = 0, rt = 0;
+    if (t < nalive) {
+        i = c.alive[t];
+        const uint8_t nb = c.nblk[i];
+        if (c.state[i] == ST_UNDECIDED && nb != 0) {
+            if (nb != NB_OVERFLOW) {
+                for (int b = 0; b < nb && !src; b++) {
+                    const int32_t e = c.blk[(uint64_t)i * NB + b];
+                    if (blk_wrapped(e)) src = c.state[blk_index(e)] == ST_UNDECIDED;  // in the pass
+                }
+            } else {
+                visit_colliders<F32>(g, geo, c, i, rt, [&](int32_t j, bool wrap) {
+                    src |= wrap && c.state[j] == ST_UNDECIDED;
+                    return src;
+                });
+            }
+        }
+    }
+    // mark after every source test of the pass has read the states it needs: sources only by the ones read
+    // here, so a separate loop writes
+    const uint32_t slot = warp_append(&c.counters[5], src);
+    if (src) frontier(c, 0)[slot] = i;
+}
+
+// marks the sources found (their states stay UNDECIDED while the sources are searched)
+__global__ void k_pass_mark(CandArgs c) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < c.counters[5]) c.state[frontier(c, 0)[t]] = ST_PASS_C;
+}
+
+// One level of the search: every Conflict candidate of frontier `from` marks the later candidates of the pass
+// that collide with it and puts them in frontier 1 - from.
+template <bool F32>
+__global__ void k_pass_push(Grid<D> g, Geo<D> geo, CandArgs c, int from) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nf = c.counters[5 + from];
+    if (t >= nf) return;
+    const uint32_t j = frontier(c, from)[t];
+    uint32_t* out = frontier(c, 1 - from);
+    uint32_t* cnt = &c.counters[5 + (1 - from)];
+    double x[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) x[d] = c.pos[(uint64_t)j * D + d];
+    const double r = c.rad[j];
+    const uint64_t key = c.key[j];
+    uint32_t rt = 0;
+    auto mark = [&](int32_t i) {
+        if (claim_conflict(c, (uint32_t)i)) out[atomicAdd(cnt, 1u)] = (uint32_t)i;
+    };
+    if constexpr (!F32) {
+        int32_t k[D];
+        cell_of<D>(g, geo, x, k);
+        visit_candidates(g, geo, c, k, nullptr, search_r2(r, cand_rmax(g, c)), [&](int32_t i, const double* img, const int8_t*) {
+            if (!precedes(key, (int32_t)j, c.key[i], (uint32_t)i)) return false;
+            if (load_state(c.state, i) != ST_UNDECIDED) return false;
+            if (collide64<D>(r, x, c.rad[i], img)) mark(i);
+            return false;
+        });
+    } else {
+        int32_t k[D];
+        float offq[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            k[d] = c.kc[(uint64_t)j * D + d];
+            offq[d] = c.off[(uint64_t)j * D + d];
+        }
+        float rf = __double2float_rn(r);
+        asm volatile("" : "+f"(rf));
+        visit_candidates_o(g, c, k, offq, search_r2f(rf, cand_rmaxf(g, c)), [&](int32_t i, const int32_t* o, const int8_t* q) {
+            if (!precedes(key, (int32_t)j, c.key[i], (uint32_t)i)) return false;
+            if (load_state(c.state, i) != ST_UNDECIDED) return false;
+            if (cand_collide32(g, geo, c, x, r, offq, rf, i, o, q, rt)) mark(i);
+            return false;
+        });
+    }
+    if (F32 && rt) atomicAdd(&c.counters[4], rt);
+}
+
+// One greedy step of a candidate of the pass that is not Conflict; returns true when it is still undecided.
 template <bool F32>
 __device__ __forceinline__ bool pass_body(const Grid<D>& g, const Geo<D>& geo, const CandArgs& c, uint32_t i,
                                           uint32_t& rt) {
     if (load_state(c.state, i) != ST_UNDECIDED) return false;
-    bool conflict = false, any_u = false, pending = false;
-    visit_colliders<F32>(g, geo, c, i, rt, [&](int32_t j, bool wrap) {
+    bool any_u = false, pending = false;
+    visit_colliders<F32>(g, geo, c, i, rt, [&](int32_t j, bool) {
         const uint8_t s = load_state(c.state, j);
-        if (s == ST_UNDECIDED || s >= ST_PASS_U) {  // j belongs to this pass
-            if (wrap || s == ST_PASS_C) conflict = true;
-            else if (s == ST_PASS_U) any_u = true;
-            else if (s == ST_UNDECIDED) pending = true;
-        }
-        return conflict;
+        any_u |= s == ST_PASS_U;
+        pending |= s == ST_UNDECIDED;
+        return any_u;
     });
-    if (conflict) c.state[i] = ST_PASS_C;
+    if (any_u) c.state[i] = ST_PASS_S;
     else if (pending) return true;
-    else c.state[i] = any_u ? ST_PASS_S : ST_PASS_U;
+    else c.state[i] = ST_PASS_U;
     return false;
 }
 
@@ -894,6 +1020,7 @@ __device__ __forceinline__ bool commit_body(const Grid<D>& g, const Geo<D>& geo,
                 if (g.off) ((float*)g.off)[idx * D + d] = __double2float_rn(__dsub_rn(x, base));
             }
             if ((D == 2 || D == 3) && g.bocc) atomicOr((unsigned long long*)g.bocc + bidx, 1ull << bbit);
+            if (D == 3 && g.bnew) atomicOr(g.bnew + bidx, 1ull << bbit);
             // a one-radius grid without per-cell radius or phase arrays (batched instances) skips them
             if (g.rad) g.rad[idx] = c.rad[i];
             if (g.radf) ((float*)g.radf)[idx] = __double2float_rn(c.rad[i]);
@@ -940,6 +1067,16 @@ struct RefineParams {
     uint64_t rho_frac[D];  // level-0 voxel length / cell edge: 64-bit fraction and integer part
     uint32_t rho_int[D];
     int32_t level;         // parent level (fixed-point shift)
+    // sphere lists handed from voxels to their children (RefineArgs)
+    int32_t record, inherit;
+    float hdiagf;
+    const uint32_t* lin;
+    const uint8_t* nin;
+    const uint32_t* parent;
+    uint32_t* lout;
+    uint8_t* nout;
+    uint32_t* parent_out;
+    uint64_t div0, div1;
 };
 
 // child index with bit d = offset along dimension d, for the child at position t of the corner table
@@ -1771,8 +1908,10 @@ constexpr int Q_WARPS = 4;
 constexpr int Q_BLOCK = 32 * Q_WARPS;
 constexpr int Q_CAP = 160;  // queued (voxel, cell) pairs per warp
 constexpr int Q_PRE = 16;   // prefilter spheres kept per voxel
+constexpr int Q_TOUCH = 8;  // recording passes: spheres kept per voxel that reach into it but are not prefilter
 constexpr int QD2 = D > 2 ? 2 : 0;  // the third dimension's index (this kernel runs for D = 3 only)
 
+template <bool LISTS>
 struct WarpQueue {
     float relc[D][32], relo[D][32];
     // one queued pair per word: cell index (bits 0-31), cell offsets + 128 (8 bits each, from bit 32), owner
@@ -1780,6 +1919,8 @@ struct WarpQueue {
     unsigned long long q[Q_CAP];
     uint32_t pcell[32][Q_PRE];
     int8_t po[32][Q_PRE][D];
+    uint32_t tcell[LISTS ? 32 : 1][Q_TOUCH];  // recording passes only
+    uint32_t ntouch[32];
     uint32_t npre[32];
     uint32_t pref[32];  // inclusive prefix of the children phase's per-lane counts
     uint32_t cov[32];
@@ -1787,11 +1928,45 @@ struct WarpQueue {
     uint32_t over;      // bit per lane: prefilter list overflow
 };
 
+// Whether the sphere at cell offset o (offsets offs, radius rs) reaches into the voxel with origin offset relo:
+// the squared distance from its centre to the voxel's nearest point below (r_s + r_min)^2, screened in FP32 with
+// twice the guard band to spare (a sphere it keeps in error only costs a test).
+__device__ __forceinline__ bool reaches32(const Grid<D>& g, const RefineParams& p, const int32_t* o,
+                                          const float* offs, float rs, const float* relo) {
+    float d0[D];
+    model_delta<D>(g.cf, o, offs, relo, d0);
+    const float R = __fadd_rn(rs, p.rminf);
+    const float hi = __fadd_rn(__fmul_rn(R, R), __fmul_rn(2.f, g.guard));
+    float m = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const float t = d0[d] < 0.f ? -d0[d] : fmaxf(__fsub_rn(d0[d], p.lenf[d]), 0.f);
+        m = __fadd_rn(m, __fmul_rn(t, t));
+    }
+    return m <= hi;
+}
+
+// Coordinates of cell idx of a 3D grid: two divisions by multiplies with ceil(2^64 / n) (exact for idx < 2^32,
+// n < 2^32, n >= 2).
+__device__ __forceinline__ void cell_coords(const Grid<D>& g, const RefineParams& p, uint32_t idx, int32_t* c) {
+    const uint32_t t = (uint32_t)__umul64hi((unsigned long long)idx, p.div0);
+    c[0] = (int32_t)(idx - t * (uint32_t)g.n[0]);
+    const uint32_t z = (uint32_t)__umul64hi((unsigned long long)t, p.div1);
+    c[1] = (int32_t)(t - z * (uint32_t)g.n[1]);
+    c[QD2] = (int32_t)z;
+}
+
 // The warp-queue pass for the 32 voxels of a warp, all lanes together (every lane calls it, active or not,
 // with the same grid): fills mask, returns true when this lane's voxel survives.  vin and vbase locate the
 // warp's voxels (their coordinates are reloaded for the guard band's retests).
+// Recording passes (p.record) reach r_s + r_min beyond the voxel's half diagonal and store, per surviving
+// voxel, its prefilter spheres and the other spheres that reach into it (RefineArgs).  Inheriting passes
+// (p.inherit) test a voxel against its parent's stored spheres and walk only the bricks of the spheres placed
+// since (g.bnew): a sphere that reaches into a voxel reaches into its parent, so it is in the parent's list
+// or new.  The decisions are those of the full walk.
+template <bool LISTS>
 __device__ __forceinline__ bool mask32q_warp(const Grid<D>& g, const Geo<D>& geo, const RefineParams& p,
-                                             WarpQueue& Q, const int64_t* vin, uint64_t vbase, bool active,
+                                             WarpQueue<LISTS>& Q, const int64_t* vin, uint64_t vbase, bool active,
                                              const int64_t* cc_in, uint32_t* mask, uint32_t& visits, uint32_t& rt) {
     const int lane = threadIdx.x & 31;
     int64_t cc[D];
@@ -1804,16 +1979,34 @@ __device__ __forceinline__ bool mask32q_warp(const Grid<D>& g, const Geo<D>& geo
         relc[d] = relo[d] = 0.f;
     }
     if (active) voxel_query32(g, p, cc, k, relc, relo);
-    const float R2q = search_r2f(p.rminf, g.rmaxf);
+    float R2q = search_r2f(p.rminf, g.rmaxf);
+    if (LISTS && p.record) {
+        const float sr = __fadd_ru(__fadd_ru(p.rminf, g.rmaxf), p.hdiagf);
+        R2q = __fmul_ru(__fmul_ru(sr, sr), 1.0001f);
+    }
     bool mine = active && brick_reach<D>(g, k, relc, R2q, lo, hi);
 #pragma unroll
     for (int d = 0; d < D; d++) mine = mine && (hi[d] >> 2) - (lo[d] >> 2) <= 1;
+    // an inherited list: the parent's spheres, then the bricks of the spheres placed since its pass
+    uint32_t ninh = 0, lbase = 0;
+    bool inh = false;
+    if (LISTS && p.inherit && mine) {
+        const uint32_t par = p.parent[vbase + lane];
+        const uint8_t cnt = p.nin[par];
+        if (cnt != LIST_NONE) {
+            inh = true;
+            ninh = cnt;
+            lbase = par * (uint32_t)LIST_K;
+        }
+    }
+    const unsigned long long* bmap = inh ? g.bnew : g.bocc;
 #pragma unroll
     for (int d = 0; d < D; d++) {
         Q.relc[d][lane] = relc[d];
         Q.relo[d][lane] = relo[d];
     }
     Q.npre[lane] = 0;
+    Q.ntouch[lane] = 0;
     Q.cov[lane] = 0;
     if (lane == 0) {
         Q.covered = 0;
@@ -1852,6 +2045,10 @@ __device__ __forceinline__ bool mask32q_warp(const Grid<D>& g, const Geo<D>& geo
             } else {
                 atomicOr(&Q.over, 1u << own);
             }
+        } else if (LISTS && p.record && reaches32(g, p, o, offs, rs, oo)) {
+            // not a prefilter sphere of this voxel, but one of a descendant's, or its cover
+            const uint32_t sl = atomicAdd(&Q.ntouch[own], 1u);
+            if (sl < Q_TOUCH) Q.tcell[own][sl] = idx;
         }
     };
     uint32_t fill = 0;  // warp-uniform
@@ -1869,6 +2066,27 @@ __device__ __forceinline__ bool mask32q_warp(const Grid<D>& g, const Geo<D>& geo
         __syncwarp();
         fill = 0;
     };
+    // inherited pairs: each lane's parent list, one entry per lane per step
+    if (LISTS && p.inherit) {
+        uint32_t mx = ninh;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        for (uint32_t j = 0; j < mx; j++) {
+            const bool has = j < ninh;
+            const uint32_t bal = __ballot_sync(0xffffffffu, has);
+            if (fill + 32 > Q_CAP) flush();
+            if (has) {
+                const uint32_t idx = p.lin[lbase + j];
+                int32_t c[D];
+                cell_coords(g, p, idx, c);
+                const uint32_t offs = (uint32_t)(c[0] - k[0] + 128) | ((uint32_t)(c[1] - k[1] + 128) << 8) |
+                                      ((uint32_t)(c[QD2] - k[QD2] + 128) << 16) | ((uint32_t)lane << 24);
+                Q.q[fill + __popc(bal & ((1u << lane) - 1u))] = (unsigned long long)idx | ((unsigned long long)offs << 32);
+            }
+            fill += __popc(bal);
+            __syncwarp();
+        }
+    }
     // visit phase: the (up to) 2 x 2 x 2 bricks of each voxel's range
     for (int sl = 0; sl < 8; sl++) {
         unsigned long long bits = 0;
@@ -1882,7 +2100,7 @@ __device__ __forceinline__ bool mask32q_warp(const Grid<D>& g, const Geo<D>& geo
                 const uint32_t ym = brick_span<2>(lo[1], hi[1], b[1]);
                 const uint32_t zm = brick_span<2>(lo[QD2], hi[QD2], b[QD2]);
                 const unsigned long long mask = brick_mask3(xm, ym, zm);
-                bits = __ldg(g.bocc + (b[0] + (int64_t)g.nb[0] * (b[1] + (int64_t)g.nb[1] * b[QD2]))) & mask;
+                bits = __ldg(bmap + (b[0] + (int64_t)g.nb[0] * (b[1] + (int64_t)g.nb[1] * b[QD2]))) & mask;
                 if ((Q.covered >> lane) & 1u) bits = 0;  // covered already: no more pairs
             }
         }
@@ -1970,6 +2188,20 @@ __device__ __forceinline__ bool mask32q_warp(const Grid<D>& g, const Geo<D>& geo
         atomicOr(&Q.cov[own], c32[0]);
     }
     __syncwarp();
+    if (LISTS && p.record && active) {
+        // this voxel's list for its children: its prefilter spheres and the others that reach into it
+        const uint64_t v = vbase + lane;
+        uint8_t n = LIST_NONE;
+        if (live) {
+            const uint32_t np = Q.npre[lane], nt = Q.ntouch[lane];
+            if (nt <= (uint32_t)Q_TOUCH && np + nt <= (uint32_t)LIST_K) {
+                for (uint32_t j = 0; j < np; j++) p.lout[v * LIST_K + j] = Q.pcell[lane][j];
+                for (uint32_t j = 0; j < nt; j++) p.lout[v * LIST_K + np + j] = Q.tcell[lane][j];
+                n = (uint8_t)(np + nt);
+            }
+        }
+        p.nout[v] = n;
+    }
 #pragma unroll
     for (int w2 = 0; w2 < MASK_WORDS; w2++) mask[w2] = 0;
     bool survived = false;
@@ -1985,15 +2217,16 @@ __device__ __forceinline__ bool mask32q_warp(const Grid<D>& g, const Geo<D>& geo
     return survived;
 }
 
+template <bool LISTS>
 __global__ void __launch_bounds__(Q_BLOCK) k_refine_mask32q(Grid<D> g, Geo<D> geo, RefineParams p) {
-    __shared__ WarpQueue wq[Q_WARPS];
+    __shared__ WarpQueue<LISTS> wq[Q_WARPS];
     const uint64_t v = (uint64_t)blockIdx.x * Q_BLOCK + threadIdx.x;
     const bool active = v < p.V;
     int64_t cc[D];
 #pragma unroll
     for (int d = 0; d < D; d++) cc[d] = active ? p.vin[v * D + d] : 0;
     uint32_t mask[MASK_WORDS], visits = 0, rt = 0;
-    const bool survived = mask32q_warp(g, geo, p, wq[threadIdx.x >> 5], p.vin, v - (threadIdx.x & 31), active, cc,
+    const bool survived = mask32q_warp<LISTS>(g, geo, p, wq[threadIdx.x >> 5], p.vin, v - (threadIdx.x & 31), active, cc,
                                        mask, visits, rt);
     mask_epilogue(p, v, active, mask, survived, visits, rt);
 }
@@ -2030,6 +2263,7 @@ __global__ void __launch_bounds__(REFINE_BLOCK) k_refine_write(RefineParams p) {
         if (!((mask[t >> 5] >> (t & 31)) & 1u)) continue;
 #pragma unroll
         for (int d = 0; d < D; d++) p.vout[o * D + d] = 2 * cc[d] + ((j >> d) & 1);
+        if (p.parent_out) p.parent_out[o] = (uint32_t)v;
         o++;
     }
 }
@@ -2154,6 +2388,8 @@ void op_darts(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaStre
     p.rand_radius = a.rand_radius;
     p.r_lo = a.r_lo;
     p.r_span = a.r_span;
+    p.rtab = a.rtab;
+    p.ntab = a.ntab;
     p.pos = c.pos;
     p.key = c.key;
     p.rad = c.rad;
@@ -2209,6 +2445,8 @@ void op_darts32(const GridArgs& ga, const CandArgs& c, const DartArgs& a, cudaSt
     p.rand_radius = a.rand_radius;
     p.r_lo = a.r_lo;
     p.r_span = a.r_span;
+    p.rtab = a.rtab;
+    p.ntab = a.ntab;
     p.pos = c.pos;
     p.key = c.key;
     p.rad = c.rad;
@@ -2275,6 +2513,21 @@ void op_pass_step(const GridArgs& ga, const CandArgs& c, int it, int f32, cudaSt
     count_launch();
 }
 
+void op_pass_sources(const GridArgs& ga, const CandArgs& c, int f32, cudaStream_t s) {
+    if (c.n == 0) return;
+    if (f32) k_pass_sources<true><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    else k_pass_sources<false><<<nblocks(c.n, 256), 256, 0, s>>>(make_grid(ga), make_geo(ga), c);
+    k_pass_mark<<<nblocks(c.n, 256), 256, 0, s>>>(c);
+    count_launch(2);
+}
+
+void op_pass_push(const GridArgs& ga, const CandArgs& c, int from, uint32_t nf, int f32, cudaStream_t s) {
+    if (nf == 0) return;
+    if (f32) k_pass_push<true><<<nblocks(nf, 128), 128, 0, s>>>(make_grid(ga), make_geo(ga), c, from);
+    else k_pass_push<false><<<nblocks(nf, 128), 128, 0, s>>>(make_grid(ga), make_geo(ga), c, from);
+    count_launch();
+}
+
 void op_pass_gather(const CandArgs& c, cudaStream_t s) {
     if (c.n == 0) return;
     k_pass_gather<<<nblocks(c.n, 256), 256, 0, s>>>(c);
@@ -2327,6 +2580,17 @@ RefineParams make_refine(const GridArgs& ga, const RefineArgs& a) {
     }
     p.level = a.level;
     p.rminf = (float)a.rmin;
+    p.record = a.record;
+    p.inherit = a.inherit;
+    p.hdiagf = a.hdiagf;
+    p.lin = a.lin;
+    p.nin = a.nin;
+    p.parent = a.parent;
+    p.lout = a.lout;
+    p.nout = a.nout;
+    p.parent_out = a.parent_out;
+    p.div0 = a.div0;
+    p.div1 = a.div1;
     return p;
 }
 
@@ -2337,7 +2601,10 @@ void op_refine_mask(const GridArgs& ga, const RefineArgs& a, int f32, cudaStream
     if (f32 && a.level == 0) {
         k_refine_mask32c<<<nblocks(a.V, COOP_BLOCK), COOP_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
     } else if (f32 && D == 3 && ga.bocc && ga.ncells < (1ll << 32)) {
-        k_refine_mask32q<<<nblocks(a.V, Q_BLOCK), Q_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
+        if (a.record)
+            k_refine_mask32q<true><<<nblocks(a.V, Q_BLOCK), Q_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
+        else
+            k_refine_mask32q<false><<<nblocks(a.V, Q_BLOCK), Q_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
     } else if (f32) {
         k_refine_mask32<<<nblocks(a.V, REFINE_BLOCK), REFINE_BLOCK, 0, s>>>(make_grid(ga), make_geo(ga), make_refine(ga, a));
     }
@@ -2416,6 +2683,8 @@ const DimOps kOps = {
     op_pass_gather,
     op_pass_close,
     op_pass_next,
+    op_pass_sources,
+    op_pass_push,
 };
 
 }  // namespace

@@ -89,6 +89,7 @@ struct Grid {
     float inv_cf[D];                 // inverse cell edges
     double rmono;
     float rmonof;
+    unsigned long long* bnew;        // bricks of the spheres placed since the last mask pass, or null
 };
 
 // ---------------------------------------------------------------------------------------------

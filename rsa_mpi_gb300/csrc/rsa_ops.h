@@ -36,6 +36,9 @@ struct GridArgs {
     double rmono;
     unsigned long long* bocc;  // 3D: occupancy by 4x4x4 bricks of cells (bit x + 4 y + 16 z), or null
     int32_t nb[MAX_D];         // bricks per dimension
+    // 3D single-instance grids: the same bricks for the spheres placed since the last mask pass (the mask pass
+    // of voxels with an inherited sphere list walks only these), or null
+    unsigned long long* bnew = nullptr;
 };
 
 struct CandArgs {
@@ -81,6 +84,9 @@ struct DartArgs {
     uint64_t* vidx_out;  // optional: chosen voxel per dart
     int32_t rand_radius;  // continuous radius law: radius = r_lo + r_span x, x from the dart's own Philox draw
     double r_lo, r_span;
+    // or, with ntab >= 2, the transform tabulated at x = j / (ntab - 1) (device array), interpolated linearly
+    const double* rtab;
+    int32_t ntab;
     uint64_t rho_frac[MAX_D];  // FP32-form darts: level-0 voxel length / cell edge (voxel_cell_ratio)
     uint32_t rho_int[MAX_D];
     int32_t level;             // voxel level (the fixed-point shift)
@@ -110,7 +116,25 @@ struct RefineArgs {
     uint64_t rho_frac[MAX_D];    // level-0 voxel length / cell edge in fixed point (voxel_cell_ratio)
     uint32_t rho_int[MAX_D];
     int32_t level;               // parent level (the fixed-point shift)
+    // Sphere lists handed from a voxel to its children (3D FP32 mask pass at levels >= 1).  A recording pass
+    // stores, for every surviving voxel, the cells of the spheres that reach into the voxel (centre within
+    // r_s + r_min of some point of it): every sphere that can cover a descendant or enter its prefilter list,
+    // among those placed so far.  An inheriting pass then tests each voxel against its parent's list plus
+    // the spheres placed since (GridArgs::bnew) instead of walking the whole neighbourhood.
+    int32_t record;              // store this pass's lists (lout, nout)
+    int32_t inherit;             // read the parents' lists (lin, nin, parent)
+    float hdiagf;                // half diagonal of this pass's voxels, rounded up (the reach of a recording walk)
+    const uint32_t* lin;         // LIST_K cell indices per voxel of the previous pass
+    const uint8_t* nin;          // their counts (LIST_NONE: no list, walk the whole neighbourhood)
+    const uint32_t* parent;      // index of each voxel's parent in the previous pass
+    uint32_t* lout;              // this pass's lists, LIST_K per voxel
+    uint8_t* nout;
+    uint32_t* parent_out;        // k_refine_write: the parent of each child written (or null)
+    uint64_t div0, div1;         // ceil(2^64 / n_0), ceil(2^64 / n_1): cell index -> coordinates
 };
+
+constexpr int LIST_K = 16;           // cells in one voxel's sphere list
+constexpr uint8_t LIST_NONE = 0xFF;  // no list: the voxel's children walk their whole neighbourhood
 
 // The FP32 form maps a point of a voxel at level `level` to cells in 64-bit fixed point:
 // y = (coordinate + u) * rho0 * 2^-level cell edges, rho0 = len0 / c (level-0 voxel length over cell edge; the
@@ -208,13 +232,17 @@ struct DimOps {
     void (*b_refine_write)(const BatchArgs& b, const RefineArgs& a, cudaStream_t s);
     void (*b_results)(const BatchArgs& b, unsigned long long* counts, unsigned long long* sums, cudaStream_t s);
     // count cap under the reference rule (the pass structure of find_solve_conflicts): the first pass's
-    // candidates, one classification step, the keys of the pass's Undecided candidates (counters[3]), the end
-    // of a pass (mode PASS_VALIDATE / PASS_PIVOT / PASS_END), and the next pass's candidates (und[0])
+    // candidates, one greedy step on the candidates that are not Conflict, the keys of the pass's Undecided
+    // candidates (counters[3]), the end of a pass (mode PASS_VALIDATE / PASS_PIVOT / PASS_END), the next pass's
+    // candidates (und[0]), the Conflict sources (frontier 0, count in counters[5]), and one level of the Conflict
+    // search (frontier `from` of nf candidates -> frontier 1 - from, count in counters[6 - from])
     void (*pass_begin)(const CandArgs& c, cudaStream_t s);
     void (*pass_step)(const GridArgs& g, const CandArgs& c, int iteration, int f32, cudaStream_t s);
     void (*pass_gather)(const CandArgs& c, cudaStream_t s);
     void (*pass_close)(const CandArgs& c, int mode, double pivot, cudaStream_t s);
     void (*pass_next)(const GridArgs& g, const CandArgs& c, int f32, cudaStream_t s);
+    void (*pass_sources)(const GridArgs& g, const CandArgs& c, int f32, cudaStream_t s);
+    void (*pass_push)(const GridArgs& g, const CandArgs& c, int from, uint32_t nf, int f32, cudaStream_t s);
 };
 
 // modes of DimOps::pass_close

@@ -59,6 +59,7 @@ struct rsagpu_radgen {
     // (radius 0, count, phase 0) in the class list, every dart's radius drawn (radius_generator.ixx:39-48)
     bool uniform = false;
     double u_rmin = 0, u_rmax = 0;
+    std::vector<double> table;  // a tabulated transform (knots at x = j / (n - 1)); empty: r_min + (r_max - r_min) x
     int u_phase = 0;
     double rmax() const { return uniform ? u_rmax : r.front(); }
     double rmin() const { return uniform ? u_rmin : r.back(); }
@@ -75,8 +76,10 @@ struct SphereGrid {
     float* d_rows_r2 = nullptr;
     int32_t* head = nullptr;
     uint32_t* cocc = nullptr;  // candidate occupancy bits of the current round
+    uint64_t nbricks = 0;      // words of a.bocc (and of a.bnew)
     void release() {
         dfree(cocc);
+        dfree(a.bnew);
         dfree(d_rows);
         dfree(d_rows_r2);
         dfree(a.off);
@@ -159,6 +162,17 @@ struct rsagpu_algo {
     uint32_t* d_err = nullptr;
     unsigned long long* d_visits = nullptr;
     uint32_t* d_sel_hist = nullptr;  // digit histogram of the count cap's radix selection
+    // sphere lists handed from voxels to their children (3D FP32 mask pass, RefineArgs): lists and counts of the
+    // voxels of vox[i], the parent of each voxel of vox[i]
+    uint32_t* lists[2] = {nullptr, nullptr};
+    uint8_t* lcount[2] = {nullptr, nullptr};
+    uint32_t* parents[2] = {nullptr, nullptr};
+    uint64_t lists_cap[2] = {0, 0}, parents_cap[2] = {0, 0};
+    bool inherit_lists = false;  // rsagpu_algo_set_inherit (measured slower on config 2, so off by default)
+    double* d_table = nullptr;  // the radius generator's tabulated transform on the device, or null
+    uint8_t* greedy_state = nullptr;  // count cap: the settle's states, kept across the passes
+    uint64_t greedy_cap = 0;
+    bool lists_ready = false;   // the last mask pass stored lists for the current voxels' parents
     uint64_t placed = 0;              // spheres in the grid
     std::vector<double> mask_ms, mask_bytes, mask_voxels;  // per refine_mask launch
     // candidates
@@ -198,6 +212,13 @@ struct rsagpu_algo {
         dfree(masks);
         dfree(block_counts);
         dfree(block_offsets);
+        dfree(d_table);
+        dfree(greedy_state);
+        for (int i = 0; i < 2; i++) {
+            dfree(lists[i]);
+            dfree(lcount[i]);
+            dfree(parents[i]);
+        }
         dfree(d_err);
         dfree(d_visits);
         dfree(d_sel_hist);
@@ -352,14 +373,19 @@ namespace {
 
 void set_device(const rsagpu_domain* d) { CK(cudaSetDevice(d->device)); }
 
+// the radius generator's tabulated transform, copied to the device (or released)
+void upload_table(rsagpu_algo* A);
+
 // a continuous radius law draws each dart's radius: r_min + (r_max - r_min) x, the span rounded first as in
 // the transform of the reference's RandomRadiusGenerator
-void set_dart_radius_law(const rsagpu_radgen& rg, DartArgs* da) {
+void set_dart_radius_law(const rsagpu_radgen& rg, const double* d_table, DartArgs* da) {
     da->rand_radius = rg.uniform ? 1 : 0;
     if (rg.uniform) {
         da->r_lo = rg.u_rmin;
         da->r_span = rg.u_rmax - rg.u_rmin;
         da->phase = rg.u_phase;
+        da->rtab = d_table;
+        da->ntab = d_table ? (int32_t)rg.table.size() : 0;
     }
 }
 
@@ -400,6 +426,8 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
     G.cocc = dalloc<uint32_t>(nwords);
     CK(cudaMemset(a.occ, 0, nwords * sizeof(uint32_t)));
     a.bocc = nullptr;
+    a.bnew = nullptr;
+    G.nbricks = 0;
     if (D == 2 || D == 3) {
         // the same occupancy by bricks of 64 cells (8x8, 4x4x4), for the brick walks
         const int side = D == 2 ? 8 : 4;
@@ -410,6 +438,12 @@ void build_grid(rsagpu_domain* dom, double rmin, double rmax) {
         }
         a.bocc = dalloc<unsigned long long>(nbricks);
         CK(cudaMemset(a.bocc, 0, nbricks * sizeof(unsigned long long)));
+        G.nbricks = nbricks;
+        if (D == 3) {
+            // the spheres placed since the last mask pass, for the sphere lists handed to the children
+            a.bnew = dalloc<unsigned long long>(nbricks);
+            CK(cudaMemset(a.bnew, 0, nbricks * sizeof(unsigned long long)));
+        }
     }
     CK(cudaMemset(G.cocc, 0, nwords * sizeof(uint32_t)));
     CK(cudaMemset(G.head, 0xFF, ncells * sizeof(int32_t)));
@@ -436,7 +470,7 @@ void ensure_cand(rsagpu_algo* A, uint64_t n) {
     C.a.rad = dalloc<double>(cap);
     C.a.phase = dalloc<int32_t>(cap);
     C.a.cell = dalloc<int64_t>(cap);
-    C.a.state = dalloc<uint8_t>(cap);
+    C.a.state = dalloc<uint8_t>((cap + 3) & ~3ull);  // whole 32-bit words (the count cap's CAS on them)
     C.a.next = dalloc<int32_t>(cap);
     C.a.alive = dalloc<uint32_t>(cap);
     C.a.blk = dalloc<int32_t>(cap * NB);
@@ -493,6 +527,7 @@ void regrid(rsagpu_algo* A, double rmin, double rmax) {
     dom->grid.a.mono = 0;
     dom->grid.a.rmono = 0;
     A->heads_dirty = false;
+    A->lists_ready = false;  // the stored lists name cells of the old grid
     if (total == 0) return;
     c.head = dom->grid.head;  // the new grid's candidate lists (the old ones were released)
     c.cocc = dom->grid.cocc;
@@ -570,6 +605,7 @@ void begin(rsagpu_algo* A) {
     A->cur = 0;
     A->V = V;
     A->level = 0;
+    A->lists_ready = false;
     A->ops->vox_init(A->vox[0], V, A->nvox0, A->stream);
     A->begun = true;
     A->round = 0;
@@ -614,10 +650,43 @@ void refine(rsagpu_algo* A) {
     r.retests = A->d_visits + 1;
     CK(cudaMemsetAsync(r.survivors, 0, sizeof(uint32_t), A->stream));
     CK(cudaMemsetAsync(r.visits, 0, 2 * sizeof(unsigned long long), A->stream));
+    // sphere lists handed to the children: the warp-queue pass of 3D FP32 grids at levels >= 1 (op_refine_mask)
+    const SphereGrid& G = A->dom->grid;
+    const bool qpath = A->form == RSAGPU_FORM_FP32_GUARD && D == 3 && G.a.bocc && G.a.bnew &&
+                       G.a.ncells < (1ll << 32) && A->level >= 1;
+    const bool record = qpath && A->inherit_lists && A->V * LIST_K < (1ull << 32) && G.a.n[0] >= 2 && G.a.n[1] >= 2;
+    const bool inherit = record && A->lists_ready;
+    if (record) {
+        const int c = A->cur;
+        if (A->V * LIST_K > A->lists_cap[c]) {
+            dfree(A->lists[c]);
+            dfree(A->lcount[c]);
+            A->lists_cap[c] = std::max<uint64_t>(A->V * LIST_K, A->lists_cap[c] + A->lists_cap[c] / 2);
+            A->lists[c] = dalloc<uint32_t>(A->lists_cap[c]);
+            A->lcount[c] = dalloc<uint8_t>(A->lists_cap[c] / LIST_K + 1);
+        }
+        r.record = 1;
+        r.lout = A->lists[c];
+        r.nout = A->lcount[c];
+        double h = 0;
+        for (int d = 0; d < D; d++) h += A->len[d] * A->len[d];
+        r.hdiagf = (float)(0.5 * std::sqrt(h) * (1 + 1e-5));
+        r.div0 = UINT64_MAX / (uint64_t)G.a.n[0] + 1;
+        r.div1 = UINT64_MAX / (uint64_t)G.a.n[1] + 1;
+        if (inherit) {
+            r.inherit = 1;
+            r.lin = A->lists[1 - c];
+            r.nin = A->lcount[1 - c];
+            r.parent = A->parents[c];
+        }
+    }
     const uint64_t nb = (A->V + 31) / 32;  // warps
     CK(cudaEventRecord(A->ev[8], A->stream));
     A->ops->refine_mask(A->dom->grid.a, r, A->form == RSAGPU_FORM_FP32_GUARD, A->stream);
     CK(cudaEventRecord(A->ev[9], A->stream));
+    // the next pass's new spheres are those placed from now on
+    if (G.a.bnew) CK(cudaMemsetAsync(G.a.bnew, 0, G.nbricks * sizeof(unsigned long long), A->stream));
+    A->lists_ready = false;
     launch_scan_blocks(A->block_counts, A->block_offsets, nb, nullptr, A->stream);
     uint64_t total = 0;
     uint32_t survivors = 0;
@@ -654,6 +723,14 @@ void refine(rsagpu_algo* A) {
     ensure_vox(A, other, total);
     r.vout = A->vox[other];
     r.vout_cap = total;
+    if (record) {
+        if (total > A->parents_cap[other]) {
+            dfree(A->parents[other]);
+            A->parents_cap[other] = std::max<uint64_t>(total, A->parents_cap[other] + A->parents_cap[other] / 2);
+            A->parents[other] = dalloc<uint32_t>(A->parents_cap[other]);
+        }
+        r.parent_out = A->parents[other];
+    }
     A->ops->refine_write(r, A->stream);
     {
         uint32_t err = 0;
@@ -664,6 +741,7 @@ void refine(rsagpu_algo* A) {
     A->cur = other;
     A->V = total;
     A->level++;
+    A->lists_ready = record;
     for (int d = 0; d < D; d++) A->len[d] = r.nlen[d];
     A->stats.refinements++;
     A->stats.peak_voxels = std::max(A->stats.peak_voxels, total);
@@ -769,23 +847,55 @@ constexpr int MAX_CAP_PASSES = 1000;
 // (median_of_medians.ixx:8-157) and the round ends.  Else the pass is validated (update_sphere_tags), the round
 // ends when the count is met exactly, and the Conflict candidates that hit no validated one make the next
 // pass.  Without a collision through the periodic boundary the first pass is the greedy set.
-void reference_cap_passes(rsagpu_algo* A, const CandArgs& c, uint64_t max_new, int f32) {
+//
+// The Undecided sets of successive passes are disjoint parts of the greedy set (whose size `greedy` the settle
+// found), and without a cut their union is the greedy set.  So once the greedy candidates not yet validated are
+// fewer than the count, no later pass can reach the count: every later pass is validated in full and the round
+// keeps the greedy set.  The passes stop there, and the greedy states saved before the first pass are restored.
+void reference_cap_passes(rsagpu_algo* A, const CandArgs& c, uint64_t max_new, uint64_t greedy, int f32) {
     const DimOps* ops = A->ops;
     const GridArgs& g = A->dom->grid.a;
     uint32_t* h = A->h_counters;
+    if (c.n > A->greedy_cap) {
+        dfree(A->greedy_state);
+        A->greedy_cap = std::max<uint64_t>(c.n, A->greedy_cap + A->greedy_cap / 2);
+        A->greedy_state = dalloc<uint8_t>(A->greedy_cap);
+    }
+    CK(cudaMemcpyAsync(A->greedy_state, c.state, c.n, cudaMemcpyDeviceToDevice, A->stream));
+    uint64_t validated = 0;
     CK(cudaMemsetAsync(c.und, 0, (MAX_SETTLE + 1) * sizeof(uint32_t), A->stream));
     ops->pass_begin(c, A->stream);
     for (int pass = 0;; pass++) {
         if (pass >= MAX_CAP_PASSES) raise(RSAGPU_ERR_NO_PROGRESS, "count cap: more than %d passes", MAX_CAP_PASSES);
+        A->stats.cap_passes++;
         CK(cudaMemcpyAsync(h + COUNTERS, c.und, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
         CK(cudaStreamSynchronize(A->stream));
         if (h[COUNTERS] == 0) break;  // no candidate left in the pass
+        // the Conflict set: its sources, then the search level by level (frontiers in counters[5], [6])
+        CK(cudaMemsetAsync(c.counters + 5, 0, 2 * sizeof(uint32_t), A->stream));
+        ops->pass_sources(g, c, f32, A->stream);
+        for (int level = 0, from = 0;; level++, from = 1 - from) {
+            if (level > MAX_SETTLE)
+                raise(RSAGPU_ERR_NO_PROGRESS, "count-cap Conflict search did not end in %d levels", MAX_SETTLE);
+            CK(cudaMemcpyAsync(h + 5 + from, c.counters + 5 + from, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                               A->stream));
+            CK(cudaStreamSynchronize(A->stream));
+            const uint32_t nf = h[5 + from];
+            if (nf == 0) break;
+            CK(cudaMemsetAsync(c.counters + 5 + (1 - from), 0, sizeof(uint32_t), A->stream));
+            ops->pass_push(g, c, from, nf, f32, A->stream);
+            A->stats.cap_steps++;
+        }
+        // the greedy on the candidates that are not Conflict, until all are classified
+        CK(cudaMemsetAsync(c.und, 0, (MAX_SETTLE + 1) * sizeof(uint32_t), A->stream));
+        CK(cudaMemsetAsync(c.und, 0x01, sizeof(uint32_t), A->stream));  // nonzero: the first step runs
         int it = 1;
         while (true) {
             for (int b = 0; b < 4; b++, it++) {
                 if (it > MAX_SETTLE)
                     raise(RSAGPU_ERR_NO_PROGRESS, "count-cap pass did not converge in %d iterations", MAX_SETTLE);
                 ops->pass_step(g, c, it, f32, A->stream);
+                A->stats.cap_steps++;
             }
             CK(cudaMemcpyAsync(h + COUNTERS + it - 1, c.und + it - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                A->stream));
@@ -809,6 +919,12 @@ void reference_cap_passes(rsagpu_algo* A, const CandArgs& c, uint64_t max_new, i
         }
         ops->pass_close(c, CAP_PASS_VALIDATE, 0.0, A->stream);
         if (nu == max_new) break;
+        validated += nu;
+        if (validated + max_new > greedy) {
+            // every later pass is validated in full: the round keeps the greedy set
+            CK(cudaMemcpyAsync(c.state, A->greedy_state, c.n, cudaMemcpyDeviceToDevice, A->stream));
+            return;
+        }
         CK(cudaMemsetAsync(c.und, 0, (MAX_SETTLE + 1) * sizeof(uint32_t), A->stream));
         ops->pass_next(g, c, f32, A->stream);
     }
@@ -890,7 +1006,7 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
                     ops->cut_accepted(c, 1, -1.0, 0, A->stream);
                 }
             } else {
-                reference_cap_passes(A, c, max_new, f32);
+                reference_cap_passes(A, c, max_new, nacc, f32);
             }
         }
     }
@@ -1059,7 +1175,7 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         da.seed = seed;
         da.round = A->round++;
         da.radius = A->rg.r[A->rg.idx];
-        set_dart_radius_law(A->rg, &da);
+        set_dart_radius_law(A->rg, A->d_table, &da);
         da.phase = A->rg.phase[A->rg.idx];
         A->cand_rmax = A->rg.uniform ? A->rg.u_rmax : da.radius;  // every dart of the round has this radius or less
         const auto tp0 = std::chrono::steady_clock::now();
@@ -1136,6 +1252,15 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
     A->stats.final_level = A->level;
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
+}
+
+void upload_table(rsagpu_algo* A) {
+    dfree(A->d_table);
+    A->d_table = nullptr;
+    const std::vector<double>& t = A->rg.table;
+    if (t.empty()) return;
+    A->d_table = dalloc<double>(t.size());
+    CK(cudaMemcpy(A->d_table, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
 }
 
 uint64_t count_spheres(rsagpu_domain* dom, rsagpu_algo* helper_none) {
@@ -1370,6 +1495,32 @@ int rsagpu_radgen_create_uniform(int dim, double r_min, double r_max, uint64_t c
     });
 }
 
+int rsagpu_radgen_create_table(int dim, const double* knots, int n_knots, uint64_t count, int phase,
+                               rsagpu_radgen** out) {
+    return guarded([&] {
+        if (!out || !knots) raise(RSAGPU_ERR_ARG, "null argument");
+        if (dim < 2 || dim > MAX_D) raise(RSAGPU_ERR_ARG, "dimension %d not supported (2..%d)", dim, MAX_D);
+        if (n_knots < 2 || n_knots > (1 << 20)) raise(RSAGPU_ERR_ARG, "need 2 to 2^20 knots, got %d", n_knots);
+        double lo = knots[0], hi = knots[0];
+        for (int j = 0; j < n_knots; j++) {
+            if (!(knots[j] > 0) || !std::isfinite(knots[j])) raise(RSAGPU_ERR_ARG, "radius must be positive");
+            lo = std::min(lo, knots[j]);
+            hi = std::max(hi, knots[j]);
+        }
+        auto* rg = new rsagpu_radgen();
+        rg->dim = dim;
+        rg->r.push_back(0.0);
+        rg->n.push_back(count);
+        rg->phase.push_back(0);
+        rg->uniform = true;
+        rg->u_rmin = lo;
+        rg->u_rmax = hi;
+        rg->u_phase = phase;
+        rg->table.assign(knots, knots + n_knots);
+        *out = rg;
+    });
+}
+
 int rsagpu_radgen_destroy(rsagpu_radgen* rg) {
     delete rg;
     return RSAGPU_OK;
@@ -1420,6 +1571,7 @@ int rsagpu_algo_create(rsagpu_domain* dom, const rsagpu_radgen* rg, int nbshots,
             dom->grid.a.rmono = rg->r.front();
             A->placed = 0;
             ensure_cand(A, 1024);
+            upload_table(A);
         } catch (...) {
             delete A;
             throw;
@@ -1443,6 +1595,14 @@ int rsagpu_algo_set_form(rsagpu_algo* algo, int form, int schedule) {
         if (schedule < 0 || schedule > RSAGPU_SCHEDULE_REFERENCE) raise(RSAGPU_ERR_ARG, "unknown schedule %d", schedule);
         algo->form = form;
         algo->schedule = schedule;
+    });
+}
+
+int rsagpu_algo_set_inherit(rsagpu_algo* algo, int on) {
+    return guarded([&] {
+        if (!algo) raise(RSAGPU_ERR_ARG, "null argument");
+        algo->inherit_lists = on != 0;
+        if (!on) algo->lists_ready = false;
     });
 }
 
@@ -1535,6 +1695,7 @@ int rsagpu_algo_reset_radgen(rsagpu_algo* algo, const rsagpu_radgen* rg) {
         algo->rmax_algo = std::max(algo->rmax_algo, rg->rmax());
         algo->rg = *rg;
         algo->rg.idx = 0;
+        upload_table(algo);
         // a smaller radius needs smaller cells (one centre per cell): regrid, keeping the spheres
         stage_grid(algo);
         if (rg->rmin() < algo->feat_rmin) {
@@ -1675,7 +1836,7 @@ int rsagpu_algo_draw_darts(rsagpu_algo* algo, uint64_t seed, uint64_t round, uin
         da.seed = seed;
         da.round = round;
         da.radius = algo->rg.r[std::min<int>(algo->rg.idx, (int)algo->rg.r.size() - 1)];
-        set_dart_radius_law(algo->rg, &da);
+        set_dart_radius_law(algo->rg, algo->d_table, &da);
         da.phase = 0;
         da.vidx_out = algo->cand.vidx;
         CandArgs c = cand_args(algo, (uint32_t)n);

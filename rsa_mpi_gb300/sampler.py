@@ -108,6 +108,20 @@ class RadiusGenerator:
         self._h = h
         return self
 
+    @classmethod
+    def transform(cls, dim: int, f, count: int = 10**16, phase: int = 0, knots: int = 4097):
+        """Continuous radius law with any transform f of x uniform in [0, 1) (the reference's
+        RandomRadiusGenerator, include/radius_generator.hxx:12-38): f is tabulated at `knots` points
+        x = j / (knots - 1) and the darts interpolate it linearly."""
+        x = np.arange(knots, dtype=np.float64) / (knots - 1)
+        t = np.ascontiguousarray([float(f(v)) for v in x], dtype=np.float64)
+        self = cls.__new__(cls)
+        self.dim = dim
+        h = C.c_void_p()
+        check(lib().rsagpu_radgen_create_table(dim, ptr(t, _lib._d), len(t), int(count), int(phase), C.byref(h)))
+        self._h = h
+        return self
+
     def __del__(self):
         if getattr(self, "_h", None):
             try:
@@ -155,6 +169,11 @@ class Algo:
 
     def set_cap_rule(self, rule: int):
         check(lib().rsagpu_algo_set_cap_rule(self._h, rule))
+
+    def set_inherit(self, on: bool = True):
+        """Sphere lists handed from voxels to their children in the FP32 3D mask pass; off (the default) walks
+        every voxel's whole neighbourhood.  Either way the decisions are the same."""
+        check(lib().rsagpu_algo_set_inherit(self._h, 1 if on else 0))
 
     def set_schedule(self, factor=0.25, min_darts=4096, max_darts=1 << 26, miss_threshold=0.99):
         check(lib().rsagpu_algo_set_schedule_params(self._h, float(factor), int(min_darts), int(max_darts),

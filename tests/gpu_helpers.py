@@ -26,6 +26,15 @@ def sort_voxels(v):
 def make_pair(case, cap_exact=False, form=0):
     """(oracle, gpu algo, gpu domain) for a golden case."""
     D = case["dim"]
+    if "table" in case:  # continuous radius law, tabulated transform
+        knots, count, ph = case["table"]
+        ora = O.Oracle.table(D, [0.0] * D, case["L"], knots, count, ph, nbshots=case["nbshots"])
+        rg = RadiusGenerator.transform(D, lambda x: float(np.interp(x, np.linspace(0, 1, len(knots)), knots)),
+                                       count, ph, knots=len(knots))
+        dom = Domain([0.0] * D, case["L"], rg.max_radius)
+        algo = Algo(dom, rg, case["nbshots"])
+        algo.set_form(form)
+        return ora, algo, dom
     if "uniform" in case:  # continuous radius law
         r0, r1, count, ph = case["uniform"]
         ora = O.Oracle.uniform(D, [0.0] * D, case["L"], r0, r1, count, ph, nbshots=case["nbshots"])

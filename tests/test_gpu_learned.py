@@ -54,20 +54,20 @@ def test_training_step_descends():
 
 @pytest.mark.skipif(not os.path.exists(S.WEIGHTS), reason="no trained weights")
 def test_trained_schedule_gain_over_heuristic():
-    """Held-out case (4D, r = 0.02: no 4D case is in the training set): same validity, certified maximal,
-    same packing statistics, and the time to maximality with the learned schedule next to the heuristic's
-    (best of 3 runs each).  Measured on GB300: 235 ms learned vs 262 ms heuristic."""
+    """Held-out case (4D, r = 0.02: no 4D case is in the training set): both schedules give valid, certified
+    maximal packings with the same statistics, and the trained network reaches maximality in less time than the
+    heuristic: the median of 5 runs at least 3 % below the heuristic's median."""
+    import statistics
     _, wb = S.load()
     case = (4, [1.0] * 4, [(0.02, 1.0, 0)])
     res = {}
     for name, sch, w in (("heuristic", _lib.RSAGPU_SCHEDULE_HEURISTIC, None), ("learned", _lib.RSAGPU_SCHEDULE_LEARNED, wb)):
-        best = None
-        for rep in range(3):
+        times = []
+        for rep in range(5):
             out = S.run_case(*case, seed=5, schedule=sch, weights_bf16=w)
             assert out["check"] == (0, 0) and out["stats"]["maximal"] == 1
-            ms = out["stats"]["ms_total"]
-            best = ms if best is None else min(best, ms)
-        res[name] = (best, out["stats"]["rounds"], out["fraction"])
-    print("learned vs heuristic:", res)
+            times.append(out["stats"]["ms_total"])
+        res[name] = (statistics.median(times), out["stats"]["rounds"], out["fraction"])
+    print("learned vs heuristic (median ms, rounds, fraction):", res)
     assert abs(res["learned"][2] - res["heuristic"][2]) < 0.005  # same packing statistics
-    assert res["learned"][0] < res["heuristic"][0]  # the network gains time over the heuristic here
+    assert res["learned"][0] < 0.97 * res["heuristic"][0]

@@ -109,6 +109,23 @@ def test_replay_polydisperse_other_seeds(name, seed, form):
 
 
 @pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
+@pytest.mark.parametrize("dim,L,lo,hi,seed", [(2, [1.0, 1.0], 0.01, 0.02, 3), (3, [1.0, 0.8, 0.6], 0.04, 0.06, 5)])
+def test_replay_tabulated_radius_law(dim, L, lo, hi, seed, form):
+    """An arbitrary transform of the reference's RandomRadiusGenerator, tabulated (log-uniform radii between lo
+    and hi at 4,097 knots): the oracle draws each round's radii from the reference's stream through the table,
+    and the GPU decides the same candidates and refines the same voxels, to maximality."""
+    knots = lo * (hi / lo) ** np.linspace(0.0, 1.0, 4097)
+    case = {"dim": dim, "nbshots": 6000, "L": L, "table": (knots, 10**16, 2)}
+    ora, algo, dom, rounds = lockstep(case, seed, form=form)
+    po, ro, fo = sort_spheres(*ora.spheres())
+    pg, rg, fg = sort_spheres(*dom.arrays())
+    np.testing.assert_array_equal(po, pg)
+    np.testing.assert_array_equal(ro, rg)
+    assert np.all(fg == 2) and ro.min() >= lo and ro.max() <= hi
+    assert len(algo.voxels()[0]) == 0 and dom.check() == (0, 0)
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["fp64", "fp32guard"])
 @pytest.mark.parametrize("dim,r,seed", [(4, 0.12, 3), (4, 0.12, 4), (5, 0.2, 3)])
 def test_replay_higher_dimensions_against_oracle(dim, r, seed, form):
     """D = 4 and 5, decision by decision and voxel set by voxel set against the oracle, to certified

@@ -83,3 +83,39 @@ def test_packing_distribution_matches_the_reference_algorithm(dim, form):
     vol = O.volume_sphere(dim, r)
     compare([len(p) * vol for p in gpu], [len(p) * vol for p in ora], "packing fraction")
     compare([normalised_g(p, r) for p in gpu], [normalised_g(p, r) for p in ora], "g(r) near contact")
+
+
+# an arbitrary radius transform, tabulated: r = 0.01 (1 + 0.05 x^2) in the 2D unit square.  (A wide radius range
+# can leave voids that only radii within a hair of the smallest fit, which both the reference's algorithm and this
+# one then refine for a very long time; the law here stays narrow.)
+LAW = 0.01 * (1.0 + 0.05 * np.linspace(0.0, 1.0, 4097) ** 2)
+RBINS = np.linspace(0.01, 0.0105, 9)
+
+
+def radius_stats(rad):
+    return np.concatenate([[np.sum(np.pi * rad ** 2)], np.histogram(rad, RBINS)[0] / len(rad)])
+
+
+@pytest.mark.parametrize("form", [_lib.RSAGPU_FORM_FP32_GUARD, _lib.RSAGPU_FORM_FP64])
+def test_tabulated_radius_law_matches_the_reference_algorithm(form):
+    """Radii drawn through a tabulated transform (the reference's RandomRadiusGenerator with an arbitrary
+    transform): the GPU's packing fraction and histogram of accepted radii against the reference's algorithm
+    with the same table, over 24 seeds each."""
+    from rsa_mpi_gb300.sampler import RadiusGenerator as RG
+    gpu, ora = [], []
+    for s in range(24):
+        rg = RG.transform(2, lambda x: 0.01 * (1.0 + 0.05 * x * x), knots=len(LAW))
+        dom = Domain([0.0, 0.0], [1.0, 1.0], rg.max_radius)
+        algo = Algo(dom, rg, 6000)
+        algo.set_form(form)
+        algo.proceed(3000 + s)
+        assert algo.stats()["maximal"] == 1
+        rad = dom.arrays()[1]
+        assert rad.min() >= 0.01 and rad.max() <= 0.0105
+        gpu.append(radius_stats(rad))
+        algo.close()
+        dom.close()
+        o = O.Oracle.table(2, [0.0, 0.0], [1.0, 1.0], LAW)
+        o.proceed(4000 + s)
+        ora.append(radius_stats(o.spheres()[1]))
+    compare(gpu, ora, "packing fraction and radius histogram")
