@@ -18,7 +18,9 @@ cpu_baseline: the oracle's C restatement of the reference (single thread) on a b
          same workload (same radius, periodic box of side 0.2 = 1/125 of the volume).
 --impl reference: the CPU path of the reference, restated by the oracle (the reference itself cannot
          be compiled on the GPU host, which has no copy of its sources): one instance per host core on
-         the bounded sample, run concurrently; the line reports their aggregate spheres/s.
+         the bounded sample, run concurrently; the line reports their aggregate spheres/s.  Against the
+         reference compiled unmodified (x86, 8 cores, same sample) the restatement ran at 1.17x the
+         reference's speed on one thread and 0.81x for 8 concurrent instances (REFERENCE_CALIBRATION).
 """
 from __future__ import annotations
 
@@ -43,6 +45,11 @@ WORKLOADS = {
     "config1": (2, [1.0, 1.0], 0.005, 0, "2D periodic unit square, r=0.005, seed 0, to certified maximality"),
 }
 CPU_SAMPLE = (3, [0.2, 0.2, 0.2], 0.002, 1)
+# the oracle's restatement against the reference itself on CPU_SAMPLE (Intel Xeon @ 2.70 GHz, 8 cores, median
+# of 3): reference 7.58 s on 1 OpenMP thread, restatement 6.49 s; 8 concurrent 1-thread instances 8.08 s
+# (reference) against 9.97 s (restatement)
+REFERENCE_CALIBRATION = {"cpu": "Intel Xeon @ 2.70 GHz, 8 cores", "port_vs_reference_1_thread": 1.17,
+                         "port_vs_reference_8_instances": 0.81}
 
 
 def env_rank():
@@ -340,7 +347,8 @@ def reference_arm(args):
         "config": {"workload": wl[4], "cpu_sample": "3D periodic box of side 0.2 (1/125 of the unit cube), r=0.002, "
                    f"one instance per core ({cores}), seeds 1000*step+i"},
         "cpu_baseline": {"value": value, "unit": "spheres/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} concurrent instances of the 3D box-0.2 r=0.002 case"},
+                         "sample": f"{cores} concurrent instances of the 3D box-0.2 r=0.002 case",
+                         "calibration": REFERENCE_CALIBRATION},
         "e2e": {"value": value, "unit": "spheres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -494,7 +502,8 @@ def main():
         n, s = cpu_sample(*CPU_SAMPLE)
         line["cpu_baseline"] = {"value": n / s, "unit": "spheres/s", "cores": 1, "kind": "port",
                                 "sample": "3D periodic box of side 0.2 (1/125 of the unit cube), r=0.002, seed 1, "
-                                          f"to certified maximality: {n} spheres in {s:.1f} s"}
+                                          f"to certified maximality: {n} spheres in {s:.1f} s",
+                                "calibration": REFERENCE_CALIBRATION}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
