@@ -152,6 +152,18 @@ inline uint64_t cap_darts(uint64_t C, uint64_t remaining, uint64_t min_darts) {
     return (double)C > cap ? (uint64_t)cap : C;
 }
 
+// Darts of a round of a class that has a count (single-instance heuristic and learned schedules): about 1.25x the
+// spheres still wanted at the hit ratio (greedy accepted / darts) of the class's previous round, or 4x the spheres
+// still wanted for the class's first round.  A round past the count is cut by the count cap, so its extra darts
+// are work thrown away (in a near-empty box nearly every dart survives the probe and enters the conflict
+// resolution); a round short of it costs one more round.  Where the count is far off (a class given by a volume
+// fraction the packing never reaches) the bound stays above the voxel-based round size.
+inline uint64_t class_darts(uint64_t C, uint64_t remaining, uint64_t min_darts, double hit_ratio) {
+    const double want = hit_ratio > 0 ? 1.25 * (double)remaining / std::max(hit_ratio, 1e-4) : 4.0 * (double)remaining;
+    const double cap = std::max(want, (double)min_darts);
+    return (double)C > cap ? (uint64_t)cap : C;
+}
+
 // miss rate of a pass (operator_algorithm.ixx:140-162): darts that placed no sphere
 inline double miss_rate(uint64_t shots, uint64_t hits) {
     return (double)(shots - hits) / (0.000001 + (double)shots);

@@ -192,6 +192,9 @@ struct rsagpu_algo {
     // learned-schedule state
     int passes_at_level = 0;
     double prev_miss = 1.0;
+    // hit ratio (greedy accepted / darts) of the last round and the class it was drawn for (class_darts)
+    double class_hit = 0.0;
+    int class_hit_idx = -1;
     uint64_t level_start_V = 0, prev_level_start_V = 0;
     // state
     bool begun = false;
@@ -590,6 +593,7 @@ void ensure_refine_buffers(rsagpu_algo* A, uint64_t V) {
 
 void begin(rsagpu_algo* A) {
     const int D = A->dom->dim;
+    A->class_hit_idx = -1;  // no hit ratio yet for the classes of this proceed
     // list_of_voxels(origin, L, r_max + r_min): n_d = 1 + int(sqrt(D) L_d / diag), len_d = L_d / n_d
     // (list_of_voxels.ixx:11-28, 192-211)
     // the algorithm's r_max is the largest over its radius generators (m_r_max, operator_algorithm.ixx:89-90,
@@ -1034,11 +1038,15 @@ void reset_counters(rsagpu_algo* A) {
 // 140-162, 190-206).  Returns true when no class is left.
 int mlp_decide_host(rsagpu_algo* A, const float* feat, bool* refine);
 
+// saturate: a round that placed more spheres than its class still wanted ends the class (the product loop).  The
+// reference subtracts in size_t (update_placed), so such an overshoot, which its count-cap pivot can leave, wraps
+// the count and the class never ends: its radius is thrown until no voxel is left and the later classes are never
+// drawn.  The replay seam keeps that arithmetic (saturate = false).
 bool end_round(rsagpu_algo* A, uint64_t n_shots, uint64_t n_new, bool* refined, double thr, uint64_t n_hits,
-               TraceRow* row = nullptr) {
+               TraceRow* row = nullptr, bool saturate = false) {
     rsagpu_radgen& rg = A->rg;
     if (rg.idx < (int)rg.n.size()) {
-        rg.n[rg.idx] = rg.n[rg.idx] - n_new;
+        rg.n[rg.idx] = saturate && n_new > rg.n[rg.idx] ? 0 : rg.n[rg.idx] - n_new;
         if (rg.n[rg.idx] == 0) {
             rg.idx++;
             if (rg.idx < (int)rg.n.size()) stage_grid(A);
@@ -1163,7 +1171,10 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         const uint64_t remaining = A->rg.n[A->rg.idx];
         uint64_t C = darts_for(A);
         // no more than 16x the spheres still wanted of this class
-        if (A->schedule != RSAGPU_SCHEDULE_REFERENCE) C = cap_darts(C, remaining, A->min_darts);
+        if (A->schedule != RSAGPU_SCHEDULE_REFERENCE) {
+            C = cap_darts(C, remaining, A->min_darts);
+            C = class_darts(C, remaining, A->min_darts, A->class_hit_idx == A->rg.idx ? A->class_hit : 0.0);
+        }
         const bool may = C >= remaining;
         ensure_cand(A, C);
         reset_counters(A);
@@ -1222,6 +1233,8 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         ev_record(A, 1);
         uint64_t n_hits = 0;
         const uint64_t n_new = decide_round(A, (uint32_t)C, remaining, may, false, &n_hits);
+        A->class_hit = (double)n_hits / (double)C;
+        A->class_hit_idx = A->rg.idx;
         if (A->timing) A->stats.ms_darts += ev_ms(A, 0, 1);
         TraceRow row{};
         row.voxels = A->V;
@@ -1232,7 +1245,7 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         bool refined = false;
         // the miss rate of the geometry: darts the count cap dropped are not misses (with 10^7-dart rounds the
         // cap would otherwise read as a miss rate near 1 and refine every round)
-        const bool done = end_round(A, C, n_new, &refined, thr, n_hits, &row);
+        const bool done = end_round(A, C, n_new, &refined, thr, n_hits, &row, true);
         CK(cudaStreamSynchronize(A->stream));
         const auto tp2 = std::chrono::steady_clock::now();
         row.pass_ms = std::chrono::duration<double, std::milli>(tp1 - tp0).count();

@@ -86,6 +86,38 @@ def test_fp32_guard_form_matches_fp64_in_higher_dimensions_and_with_classes(dim,
         assert O.uncovered_after_refinement(dim, [0.0] * dim, L, out[1][0], out[1][1], r, r, 40) == 0
 
 
+def test_class_overshoot_ends_the_class():
+    """A capped round under the reference's pivot rule can keep more spheres than its class still wants (here the
+    first round of the 0.004 class, in some of the seeds).  The product loop then ends the class and draws the
+    next ones; the reference's size_t count would wrap and throw the first radius until no voxel is left.  Scaled
+    config 3 (box side 0.25: 1/64 of its volume), both forms, four seeds."""
+    classes = [(0.004, 0.20, 0), (0.002, 0.10, 0), (0.001, 0.05, 0)]
+    side = 0.25
+    targets = [int(side ** 3 * f / O.volume_sphere(3, r)) for r, f, _ in classes]
+    overshoots = 0
+    for seed in (1, 2, 3, 4):
+        out = []
+        for form in (_lib.RSAGPU_FORM_FP64, _lib.RSAGPU_FORM_FP32_GUARD):
+            rg = RadiusGenerator(3, classes, volume=side ** 3)
+            dom = Domain([0.0] * 3, [side] * 3, rg.max_radius)
+            algo = Algo(dom, rg, 6000)
+            algo.set_form(form)
+            algo.proceed(seed)
+            pos, rad, _ = dom.arrays()
+            assert dom.check() == (0, 0)
+            out.append((pos, rad))
+            algo.close()
+            dom.close()
+        np.testing.assert_array_equal(out[0][0], out[1][0])
+        rad = out[1][1]
+        per_class = [int(np.count_nonzero(rad == r)) for r, _, _ in classes]
+        assert per_class[0] >= targets[0] and per_class[1:] == targets[1:], (seed, per_class, targets)
+        assert per_class[0] <= targets[0] * 1.02
+        overshoots += per_class[0] > targets[0]
+        assert O.count_overlaps(3, [0.0] * 3, [side] * 3, out[1][0], rad) == 0
+    assert overshoots >= 1  # the case this test is about occurred
+
+
 @pytest.mark.parametrize("L,r,seed", [([1.0] * 3, 0.01, 3), ([0.6, 0.5, 0.4], 0.006, 4), ([1.0] * 3, 0.005, 5)])
 def test_inherited_sphere_lists_give_the_full_walk_result(L, r, seed):
     """FP32 form, 3D: the mask pass hands each surviving voxel's nearby spheres to its children, which test those
