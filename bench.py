@@ -355,6 +355,58 @@ def reference_arm(args):
     return 0
 
 
+def idle_report(args):
+    """GPU busy and idle time (the union of the kernel, memcpy and memset intervals of every stream, and the gaps
+    between them) over one run of the workload and one batched run of config 4, each after a warm-up run.  The
+    gaps are where the GPU waited on the host: launch latency and the round loop's readbacks.  Records come from
+    CUPTI (rsa_mpi_gb300/csrc/activity.cpp), which adds its own small overhead: these runs are not bench values."""
+    import ctypes as C
+    import torch
+    from rsa_mpi_gb300 import build as B
+    B.build()
+    so = B.build_activity()
+    if so is None:
+        print(json.dumps({"gpu_idle": None, "why": "no CUPTI in this CUDA toolkit"}))
+        return
+    act = C.CDLL(so)
+    act.rsa_activity_stop.argtypes = [C.POINTER(C.c_double)]
+    from rsa_mpi_gb300.sampler import batch_run
+
+    def measure(fn):
+        torch.cuda.synchronize()
+        rc = act.rsa_activity_start()
+        if rc != 0:
+            return {"error": f"CUPTI error {rc}"}
+        extra = fn()
+        torch.cuda.synchronize()
+        o = (C.c_double * 8)()
+        act.rsa_activity_stop(o)
+        span, busy = o[1], o[2]
+        return {"records": int(o[0]), "span_ms": span * 1e-6, "busy_ms": busy * 1e-6, "idle_ms": (span - busy) * 1e-6,
+                "idle_frac": (span - busy) / span if span else None, "gaps": int(o[3]),
+                "gap_median_us": o[4] * 1e-3, "gap_p99_us": o[5] * 1e-3, "gap_max_us": o[6] * 1e-3,
+                "gaps_over_10us_ms": o[7] * 1e-6, **extra}
+
+    dim, L, r, seed, desc = WORKLOADS[args.workload]
+    run_gpu_step(dim, L, r, seed, args.form)
+
+    def one():
+        n, st, _, _, _ = run_gpu_step(dim, L, r, seed, args.form)
+        return {"spheres": int(n), "proceed_ms": st["ms_total"], "rounds": st["rounds"]}
+
+    inst = config4_instances()
+    batch_run(inst[::16], form=1)
+
+    def batched():
+        res = batch_run(inst, form=1)
+        st = res["stats"]
+        return {"instances": len(inst), "seconds": st["seconds"], "launches": st["launches"],
+                "rounds": st["rounds"], "waves": st["waves"]}
+
+    print(json.dumps({"gpu_idle": {args.workload: {"workload": desc, **measure(one)},
+                                   "config4 (batched)": measure(batched)}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -365,9 +417,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", type=int, default=1, choices=[0, 1], help="0 = plain FP64, 1 = FP32 + guard band")
     ap.add_argument("--no-forms", action="store_true", help="skip the per-form comparison runs")
+    ap.add_argument("--idle", action="store_true",
+                    help="only report the GPU's busy and idle time over one run of the workload and of config 4 "
+                         "(CUPTI activity records), one JSON line")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.idle:
+        return idle_report(args)
 
     rank, world, local = env_rank()
     import torch

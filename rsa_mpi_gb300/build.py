@@ -18,6 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "librsagpu.so")
 CLI = os.path.join(OUT, "rsa")  # the command-line sampler (csrc/rsa_cli.cpp), linked against LIB
+ACTIVITY = os.path.join(OUT, "libactivity.so")  # GPU idle meter for bench.py --idle (csrc/activity.cpp, CUPTI)
 DIMS = (2, 3, 4, 5, 6, 7)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no multiply-add contraction anywhere; the FP64 decisions also use explicit _rn intrinsics.
@@ -61,7 +62,28 @@ def build_cli() -> str:
     return CLI
 
 
+def build_activity() -> str | None:
+    """g++ build of the CUPTI activity meter (bench.py --idle); None where the toolkit has no CUPTI."""
+    src = os.path.join(CSRC, "activity.cpp")
+    if os.path.exists(ACTIVITY) and os.path.getmtime(ACTIVITY) >= os.path.getmtime(src):
+        return ACTIVITY
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    inc, libdir = os.path.join(cuda, "include"), os.path.join(cuda, "lib64")
+    if not os.path.exists(os.path.join(inc, "cupti.h")):
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    tmp = ACTIVITY + ".tmp"
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", f"-I{inc}", src, "-o", tmp, f"-L{libdir}",
+                        "-lcupti", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(f"activity meter not built (bench.py --idle unavailable):\n{r.stderr}")
+        return None
+    os.replace(tmp, ACTIVITY)
+    return ACTIVITY
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
+    build_activity()
     if not force and up_to_date():
         return LIB
     lib_fresh = os.path.exists(LIB) and all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in _sources())

@@ -56,3 +56,12 @@ def test_python_module_mirrors_reference_names():
     assert callable(m.set_nb_threads)
     s = m.sphere_3D([0.1, 0.2, 0.3], 0.05, 2)
     assert s.center == [0.1, 0.2, 0.3] and s.radius == 0.05 and s.phase == 2
+
+
+def test_activity_meter_builds_and_exports_its_entry_points():
+    """bench.py --idle's CUPTI meter (csrc/activity.cpp): built beside the library where the toolkit has CUPTI."""
+    path = B.build_activity()
+    if path is None:
+        pytest.skip("no CUPTI in this CUDA toolkit")
+    L = C.CDLL(path)
+    assert hasattr(L, "rsa_activity_start") and hasattr(L, "rsa_activity_stop")
