@@ -72,7 +72,7 @@ def build_activity() -> str | None:
     if not os.path.exists(os.path.join(inc, "cupti.h")):
         return None
     os.makedirs(OUT, exist_ok=True)
-    tmp = ACTIVITY + ".tmp"
+    tmp = f"{ACTIVITY}.{os.getpid()}.tmp"  # builds running side by side each write their own
     r = subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", f"-I{inc}", src, "-o", tmp, f"-L{libdir}",
                         "-lcupti", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
     if r.returncode != 0:

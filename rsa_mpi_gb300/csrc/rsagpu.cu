@@ -563,10 +563,11 @@ void stage_grid(rsagpu_algo* A) {
     if (want < A->dom->grid.rmin) regrid(A, want, A->dom->grid.rmax);
 }
 
-void ensure_vox(rsagpu_algo* A, int which, uint64_t n) {
+// Voxel list `which` holds at least n voxels (and `reserve`, when it has to grow).
+void ensure_vox(rsagpu_algo* A, int which, uint64_t n, uint64_t reserve = 0) {
     const int D = A->dom->dim;
     if (n <= A->vox_cap[which]) return;
-    uint64_t cap = std::max<uint64_t>(n, A->vox_cap[which] + A->vox_cap[which] / 2);
+    uint64_t cap = std::max<uint64_t>({n, reserve, A->vox_cap[which] + A->vox_cap[which] / 2});
     dfree(A->vox[which]);
     A->vox[which] = dalloc<int64_t>(cap * D);
     A->vox_cap[which] = cap;
@@ -605,7 +606,10 @@ void begin(rsagpu_algo* A) {
         A->len[d] = A->dom->L[d] / (double)A->nvox0[d];
         V *= (uint64_t)A->nvox0[d];
     }
-    ensure_vox(A, 0, V);
+    // twice the lattice: the list refilled at the second refinement (whose voxels outnumber the lattice's in 3D,
+    // 1.5x at r = 0.002) then fits without a reallocation inside the run.  Growing it there cost a fresh mapping
+    // of about 3 GB (2.5 ms with the GPU idle), as the memory pool had split the block of the previous run's size.
+    ensure_vox(A, 0, V, 2 * V);
     A->cur = 0;
     A->V = V;
     A->level = 0;
