@@ -42,6 +42,10 @@ constexpr int NFEAT = 16;
 
 constexpr int MAX_SETTLE = 4096;
 constexpr int COUNTERS = 8;
+// pinned mirror of the counters: COUNTERS + und[MAX_SETTLE + 1], then a copy of the settle's und[] kept for the
+// round's statistics (read with the commit's counters, not in a synchronisation of its own)
+constexpr int H_COUNTERS = COUNTERS + 2 * (MAX_SETTLE + 1);
+constexpr int H_SETTLE = COUNTERS + MAX_SETTLE + 1;
 
 }  // namespace
 
@@ -459,7 +463,7 @@ void ensure_cand(rsagpu_algo* A, uint64_t n) {
     if (!C.a.counters) {
         C.a.counters = dalloc<uint32_t>(COUNTERS + MAX_SETTLE + 1);
         A->h_counters = nullptr;
-        CK(cudaMallocHost(&A->h_counters, (COUNTERS + MAX_SETTLE + 1) * sizeof(uint32_t)));
+        CK(cudaMallocHost(&A->h_counters, H_COUNTERS * sizeof(uint32_t)));
     }
     if (n <= C.cap) return;
     uint32_t* keep = C.a.counters;
@@ -630,6 +634,10 @@ void begin(rsagpu_algo* A) {
 }
 
 // remove_covered + subdivide_uncovered (list_of_voxels.ixx:30-100)
+void check_write_bounds(uint32_t err) {
+    if (err & ERR_WRITE_BOUNDS) raise(RSAGPU_ERR_INVARIANT, "refinement offsets beyond the output list");
+}
+
 void refine(rsagpu_algo* A) {
     const int D = A->dom->dim;
     if (A->V == 0) return;
@@ -697,13 +705,15 @@ void refine(rsagpu_algo* A) {
     A->lists_ready = false;
     launch_scan_blocks(A->block_counts, A->block_offsets, nb, nullptr, A->stream);
     uint64_t total = 0;
-    uint32_t survivors = 0;
+    uint32_t err_surv[2] = {0, 0};  // error bits (of this mask pass and of the earlier write passes), survivors
     unsigned long long visits = 0, retests = 0;
     CK(cudaMemcpyAsync(&retests, r.retests, sizeof(unsigned long long), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaMemcpyAsync(&total, A->block_offsets + nb, sizeof(uint64_t), cudaMemcpyDeviceToHost, A->stream));
-    CK(cudaMemcpyAsync(&survivors, r.survivors, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
+    CK(cudaMemcpyAsync(err_surv, r.err, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaMemcpyAsync(&visits, r.visits, sizeof(unsigned long long), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaStreamSynchronize(A->stream));
+    check_write_bounds(err_surv[0]);
+    const uint32_t survivors = err_surv[1];
     A->stats.retests += retests;
     {
         // the mask pass of this launch: its device time and algorithmic bytes (each logical element once:
@@ -739,13 +749,9 @@ void refine(rsagpu_algo* A) {
         }
         r.parent_out = A->parents[other];
     }
+    // its bound check (ERR_WRITE_BOUNDS in the error word) is read with the next readback of the error word: the
+    // next refinement's, or the end of proceed (a write past the list is skipped, never made)
     A->ops->refine_write(r, A->stream);
-    {
-        uint32_t err = 0;
-        CK(cudaMemcpyAsync(&err, r.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
-        CK(cudaStreamSynchronize(A->stream));
-        if (err & ERR_WRITE_BOUNDS) raise(RSAGPU_ERR_INVARIANT, "refinement offsets beyond the output list");
-    }
     A->cur = other;
     A->V = total;
     A->level++;
@@ -989,12 +995,8 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
         if (A->timing) A->stats.ms_settle += ev_ms(A, 10, 11);
         if (A->h_counters[COUNTERS + it - 1] == 0) break;
     }
-    // settle iterations actually needed: the first zero counter
-    CK(cudaMemcpyAsync(A->h_counters + COUNTERS, c.und, sizeof(uint32_t) * it, cudaMemcpyDeviceToHost, A->stream));
-    CK(cudaStreamSynchronize(A->stream));
-    int used = 0;
-    while (used < it && A->h_counters[COUNTERS + used] != 0) used++;
-    A->stats.settle_iterations += used;
+    // settle iterations actually needed (the first zero counter): counted after the commit's readback
+    CK(cudaMemcpyAsync(A->h_counters + H_SETTLE, c.und, sizeof(uint32_t) * it, cudaMemcpyDeviceToHost, A->stream));
     ev_record(A, 4);
     uint64_t greedy = 0;
     if (may_outreach) {
@@ -1023,6 +1025,9 @@ uint64_t decide_round(rsagpu_algo* A, uint32_t n, uint64_t max_new, bool may_out
     ev_record(A, 5);
     CK(cudaMemcpyAsync(A->h_counters, c.counters, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, A->stream));
     CK(cudaStreamSynchronize(A->stream));
+    int used = 0;
+    while (used < it && A->h_counters[H_SETTLE + used] != 0) used++;
+    A->stats.settle_iterations += used;
     A->stats.retests += A->h_counters[4];
     if (n_greedy) *n_greedy = may_outreach ? greedy : A->h_counters[1];
     if (A->h_counters[2] & ERR_DOUBLE_OCCUPANCY)
@@ -1263,6 +1268,11 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
     }
     CK(cudaEventRecord(t1, A->stream));
     CK(cudaEventSynchronize(t1));
+    if (A->d_err) {
+        uint32_t err = 0;
+        CK(cudaMemcpy(&err, A->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        check_write_bounds(err);
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, t0, t1);
     A->stats.ms_total += ms;
@@ -1800,6 +1810,11 @@ int rsagpu_algo_end_round(rsagpu_algo* algo, uint64_t n_shots, uint64_t n_new, i
         bool r = false;
         const bool dn = end_round(algo, n_shots, n_new, &r, reference_miss_threshold(algo->dom->dim), n_new);
         CK(cudaStreamSynchronize(algo->stream));
+        if (r) {
+            uint32_t err = 0;
+            CK(cudaMemcpy(&err, algo->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            check_write_bounds(err);
+        }
         if (refined) *refined = r;
         if (done) *done = dn;
     });
@@ -1812,6 +1827,9 @@ int rsagpu_algo_refine(rsagpu_algo* algo) {
         set_device(algo->dom);
         refine(algo);
         CK(cudaStreamSynchronize(algo->stream));
+        uint32_t err = 0;
+        CK(cudaMemcpy(&err, algo->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        check_write_bounds(err);
     });
 }
 
