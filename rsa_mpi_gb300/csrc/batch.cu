@@ -643,7 +643,17 @@ int rsagpu_batch_run(const rsagpu_instance_desc* inst, int n, int form, uint64_t
         CK(cudaGetDevice(&device));
         size_t free_b = 0, total_b = 0;
         CK(cudaMemGetInfo(&free_b, &total_b));
-        const double budget = max_bytes ? (double)max_bytes : 0.6 * (double)free_b;
+        // memory the device's pool holds but no allocation uses (freed by earlier runs of this process) is free
+        // to the allocations too, though cudaMemGetInfo counts it as used
+        uint64_t pool_reserved = 0, pool_used = 0;
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &pool_reserved);
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &pool_used);
+        }
+        cudaGetLastError();
+        const double pool_free = pool_reserved > pool_used ? (double)(pool_reserved - pool_used) : 0.0;
+        const double budget = max_bytes ? (double)max_bytes : 0.6 * ((double)free_b + pool_free);
         cudaStream_t st = nullptr;
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         struct StreamGuard {
