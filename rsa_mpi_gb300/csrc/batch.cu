@@ -44,6 +44,7 @@ struct Inst {
     double est_bytes = 0;
     // run state
     uint64_t V = 0, remaining = 0, placed = 0, C = 0;
+    double alive_ratio = 1.0;  // survivors of the probe / darts in the instance's last round (alive_darts)
     int level = 0;
     double len[MAX_D]{};
     bool refine = false;
@@ -69,6 +70,7 @@ struct Wave {
     uint64_t* new_off = nullptr;
     uint64_t* word_off = nullptr;
     uint32_t* acc = nullptr;
+    uint32_t* alive_inst = nullptr;
     unsigned long long* counts = nullptr;
     unsigned long long* sums = nullptr;
     int64_t* vox[2] = {nullptr, nullptr};
@@ -104,6 +106,7 @@ struct Wave {
         dfree(new_off);
         dfree(word_off);
         dfree(acc);
+        dfree(alive_inst);
         dfree(counts);
         dfree(sums);
         dfree(vox[0]);
@@ -324,6 +327,7 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
     W.new_off = dalloc<uint64_t>(M + 1);
     W.word_off = dalloc<uint64_t>(M + 1);
     W.acc = dalloc<uint32_t>(M);
+    W.alive_inst = dalloc<uint32_t>(M);
     W.counts = dalloc<unsigned long long>(M);
     W.sums = dalloc<unsigned long long>(M);
     W.err = dalloc<uint32_t>(2);
@@ -342,6 +346,7 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
     b.word_off = W.word_off;
     b.cinst = nullptr;
     b.acc = W.acc;
+    b.alive_inst = W.alive_inst;
     b.nwords = nwords;
     b.occ = W.occ;
     b.pos = W.pos;
@@ -358,7 +363,8 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
     uint32_t* h_acc = nullptr;
     uint32_t* h_cnt = nullptr;
     uint64_t* h_off = nullptr;
-    CK(cudaMallocHost(&h_acc, M * sizeof(uint32_t)));
+    CK(cudaMallocHost(&h_acc, 2 * (size_t)M * sizeof(uint32_t)));  // accepted, then survivors, per instance
+    uint32_t* h_alive = h_acc + M;
     struct HostFree {
         void* p;
         ~HostFree() {
@@ -382,6 +388,7 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
             any = true;
             x.C = cap_darts(heuristic_darts(kDefaultFactor, kDefaultMinDarts, kDefaultMaxDarts, x.V), x.remaining,
                             kDefaultMinDarts);
+            x.C = alive_darts(x.C, x.V, x.alive_ratio);
         }
         if (!any) break;
         dart_off[0] = 0;
@@ -407,6 +414,7 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
         CK(cudaMemcpyAsync(W.dart_off, dart_off.data(), (M + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
         CK(cudaMemsetAsync(W.c.counters, 0, (B_COUNTERS + B_MAX_SETTLE + 1) * sizeof(uint32_t), st));
         CK(cudaMemsetAsync(W.acc, 0, M * sizeof(uint32_t), st));
+        CK(cudaMemsetAsync(W.alive_inst, 0, M * sizeof(uint32_t), st));
         CandArgs c = W.c;
         c.n = (uint32_t)ndarts;
         c.head = nullptr;  // per instance, from the table
@@ -463,6 +471,7 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
         ops->b_commit(b, c, st);
         CK(cudaMemcpyAsync(h_cnt, c.counters, B_COUNTERS * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(h_acc, W.acc, M * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(h_alive, W.alive_inst, M * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         if (h_cnt[2] & ERR_DOUBLE_OCCUPANCY) raise(RSAGPU_ERR_INVARIANT, "two accepted centres in one grid cell");
         if (h_cnt[2] & ERR_DART_SLOT) raise(RSAGPU_ERR_INVARIANT, "binned dart order: a bin overflowed");
@@ -481,6 +490,7 @@ void run_wave(int D, const DimOps* ops, std::vector<Inst*>& I, bool f32, Tuner& 
             Inst& x = *I[s];
             if (x.done) continue;
             const uint64_t a = h_acc[s];
+            x.alive_ratio = x.C ? (double)h_alive[s] / (double)x.C : 1.0;
             if (a > x.remaining)
                 raise(RSAGPU_ERR_STATE, "instance %d: the count cap binds (batched instances target fraction 1)",
                       x.user);
@@ -631,6 +641,7 @@ int rsagpu_batch_run(const rsagpu_instance_desc* inst, int n, int form, uint64_t
             // compute_desired_radius_nb_phase with volume fraction 1 (radius_generator.ixx:71-86)
             x.target = (uint64_t)(vol * 1.0 / ball_volume(d.dim, d.radius));
             x.remaining = x.target;
+            x.alive_ratio = 1.0;
             x.V = x.V0;
             const int D = d.dim;
             const double Vpeak = PEAK_VOXELS_PER_LEVEL0 * (double)x.V0;

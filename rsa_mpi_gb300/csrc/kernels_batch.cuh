@@ -139,8 +139,9 @@ __global__ void __launch_bounds__(512, 2) k_b_probe(BatchArgs b, CandArgs c) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t rt = 0;
     bool alive = false;
+    uint32_t s = 0xffffffffu;
     if (i < c.n && c.state[i] == ST_UNDECIDED) {
-        const uint32_t s = b.cinst[i];
+        s = b.cinst[i];
         const BInst& I = ((const BInst*)b.table)[s];
         const Grid<D>& g = I.g;
         const Geo<D>& geo = I.geo;
@@ -148,6 +149,9 @@ __global__ void __launch_bounds__(512, 2) k_b_probe(BatchArgs b, CandArgs c) {
     }
     const uint32_t slot = warp_append(&c.counters[0], alive);
     if (alive) c.alive[slot] = i;
+    // survivors per instance (the next round's size, alive_darts): one atomic per instance present in the warp
+    const uint32_t peers = __match_any_sync(0xffffffffu, alive ? s : 0xffffffffu);
+    if (alive && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&b.alive_inst[s], (uint32_t)__popc(peers));
     if (F32) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) rt += __shfl_xor_sync(0xffffffffu, rt, o);

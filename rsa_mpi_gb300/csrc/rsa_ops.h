@@ -182,6 +182,7 @@ struct BatchArgs {
     const int64_t* vox;        // the wave's voxel list (D coordinates per voxel)
     uint32_t* cinst;           // instance of each candidate
     uint32_t* acc;             // spheres accepted per instance in the current round
+    uint32_t* alive_inst;      // candidates per instance that survived the probe in the current round
     uint64_t round;            // round index (the Philox counter's round words)
     uint32_t* bin_hist;        // binned dart order over the wave's voxel list (see DartArgs), or null
     const uint64_t* bin_off;   // null in pass 1

@@ -199,6 +199,7 @@ struct rsagpu_algo {
     // hit ratio (greedy accepted / darts) of the last round and the class it was drawn for (class_darts)
     double class_hit = 0.0;
     int class_hit_idx = -1;
+    double alive_ratio = 1.0;  // survivors of the probe / darts, last round (alive_darts)
     uint64_t level_start_V = 0, prev_level_start_V = 0;
     // state
     bool begun = false;
@@ -599,6 +600,7 @@ void ensure_refine_buffers(rsagpu_algo* A, uint64_t V) {
 void begin(rsagpu_algo* A) {
     const int D = A->dom->dim;
     A->class_hit_idx = -1;  // no hit ratio yet for the classes of this proceed
+    A->alive_ratio = 1.0;   // the first round: every dart may survive
     // list_of_voxels(origin, L, r_max + r_min): n_d = 1 + int(sqrt(D) L_d / diag), len_d = L_d / n_d
     // (list_of_voxels.ixx:11-28, 192-211)
     // the algorithm's r_max is the largest over its radius generators (m_r_max, operator_algorithm.ixx:89-90,
@@ -1183,6 +1185,7 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         if (A->schedule != RSAGPU_SCHEDULE_REFERENCE) {
             C = cap_darts(C, remaining, A->min_darts);
             C = class_darts(C, remaining, A->min_darts, A->class_hit_idx == A->rg.idx ? A->class_hit : 0.0);
+            C = alive_darts(C, A->V, A->alive_ratio);
         }
         const bool may = C >= remaining;
         ensure_cand(A, C);
@@ -1244,6 +1247,7 @@ void proceed(rsagpu_algo* A, uint64_t seed) {
         const uint64_t n_new = decide_round(A, (uint32_t)C, remaining, may, false, &n_hits);
         A->class_hit = (double)n_hits / (double)C;
         A->class_hit_idx = A->rg.idx;
+        A->alive_ratio = (double)A->h_counters[0] / (double)C;
         if (A->timing) A->stats.ms_darts += ev_ms(A, 0, 1);
         TraceRow row{};
         row.voxels = A->V;
