@@ -2359,6 +2359,57 @@ __global__ void __launch_bounds__(OCC_BLOCK) k_extract_write(Grid<D> g, const ui
     }
 }
 
+// The same output as k_extract_write, each warp's spheres written as contiguous runs: the warp's occupied cells
+// (its 32 words, in order) are handed out one per lane (owner lane by binary search over the warp's inclusive
+// counts, the cell by the rank of its bit), then every array is stored lane after lane.  For outputs in pinned host
+// memory, which the kernel writes across the chip-to-host link: whole lines instead of one short run per thread.
+__global__ void __launch_bounds__(OCC_BLOCK) k_extract_direct(Grid<D> g, const uint64_t* block_offsets, double* pos,
+                                                            double* rad, int32_t* phase) {
+    constexpr uint32_t FULL = 0xffffffffu;
+    const int64_t nwords = (g.ncells + 31) / 32;
+    const int64_t w = (int64_t)blockIdx.x * OCC_BLOCK + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const uint32_t bits = w < nwords ? g.occ[w] : 0u;
+    const uint32_t c = (uint32_t)__popc(bits);
+    const uint32_t local = block_exclusive_scan<OCC_BLOCK>(c, nullptr);
+    const uint64_t wbase = block_offsets[blockIdx.x] + __shfl_sync(FULL, local, 0);  // the warp's first output
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    for (uint32_t e0 = 0; e0 < total; e0 += 32) {
+        const uint32_t e = e0 + lane;
+        const uint32_t n = total - e0 < 32 ? total - e0 : 32;  // spheres in this step (warp-uniform)
+        int own = 0;  // the lane whose inclusive count first exceeds e
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const uint32_t v = __shfl_sync(FULL, incl, own + step - 1);
+            if (v <= e) own += step;
+        }
+        own = own < 31 ? own : 31;
+        const uint32_t ob = __shfl_sync(FULL, bits, own), oc = __shfl_sync(FULL, c, own);
+        const uint32_t oi = __shfl_sync(FULL, incl, own);
+        const uint32_t rank = e - (oi - oc);
+        int64_t idx = 0;
+        if (e < total) idx = ((int64_t)blockIdx.x * OCC_BLOCK + (threadIdx.x & ~31u) + own) * 32 + (__fns(ob, 0, (int)rank + 1));
+        if (pos) {
+            // n spheres x D coordinates, stored lane after lane
+            for (uint32_t k = lane; k < ((n * D + 31u) & ~31u); k += 32) {
+                const uint32_t sph = k / D, d = k - sph * D;
+                const int64_t src = __shfl_sync(FULL, idx, (int)(sph < 32 ? sph : 31));
+                if (k < n * D) pos[(wbase + e0) * D + k] = g.pos[src * D + d];
+            }
+        }
+        if (e < total) {
+            if (rad) rad[wbase + e] = g.rad[idx];
+            if (phase) phase[wbase + e] = g.phase[idx];
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // host launchers
 // ------------------------------------------------------------------------------------------------
@@ -2643,6 +2694,13 @@ void op_extract_write(const GridArgs& ga, const uint64_t* block_offsets, double*
     count_launch();
 }
 
+void op_extract_direct(const GridArgs& ga, const uint64_t* block_offsets, double* pos, double* rad, int32_t* phase,
+                       cudaStream_t s) {
+    const int64_t nwords = (ga.ncells + 31) / 32;
+    k_extract_direct<<<nblocks(nwords, OCC_BLOCK), OCC_BLOCK, 0, s>>>(make_grid(ga), block_offsets, pos, rad, phase);
+    count_launch();
+}
+
 #include "kernels_batch.cuh"
 
 const DimOps kOps = {
@@ -2685,6 +2743,7 @@ const DimOps kOps = {
     op_pass_next,
     op_pass_sources,
     op_pass_push,
+    op_extract_direct,
 };
 
 }  // namespace

@@ -244,6 +244,10 @@ struct DimOps {
     void (*pass_next)(const GridArgs& g, const CandArgs& c, int f32, cudaStream_t s);
     void (*pass_sources)(const GridArgs& g, const CandArgs& c, int f32, cudaStream_t s);
     void (*pass_push)(const GridArgs& g, const CandArgs& c, int from, uint32_t nf, int f32, cudaStream_t s);
+    // extract_write into outputs the kernels can store to directly (pinned host memory): each warp writes its
+    // spheres as contiguous runs of the output arrays
+    void (*extract_direct)(const GridArgs& g, const uint64_t* block_offsets, double* pos, double* rad,
+                           int32_t* phase, cudaStream_t s);
 };
 
 // modes of DimOps::pass_close

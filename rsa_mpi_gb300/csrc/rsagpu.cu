@@ -1453,6 +1453,24 @@ int rsagpu_domain_extract(rsagpu_domain* dom, double* centers, double* radii, in
             dfree(offs);
             return;
         }
+        // outputs in pinned host memory that the device can store to at the same address: written there directly
+        // (no device staging, no copies)
+        auto mapped = [](const void* p) {
+            if (!p) return true;
+            cudaPointerAttributes at{};
+            if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+                cudaGetLastError();
+                return false;
+            }
+            return at.type == cudaMemoryTypeHost && at.devicePointer == p;
+        };
+        if (mapped(centers) && mapped(radii) && mapped(phases)) {
+            dim_ops(D)->extract_direct(g, offs, centers, radii, phases, dom->stream);
+            CK(cudaStreamSynchronize(dom->stream));
+            dfree(counts);
+            dfree(offs);
+            return;
+        }
         double* dp = centers ? dalloc<double>(total * D) : nullptr;
         double* dr = radii ? dalloc<double>(total) : nullptr;
         int32_t* dph = phases ? dalloc<int32_t>(total) : nullptr;

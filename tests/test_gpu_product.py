@@ -86,6 +86,39 @@ def test_fp32_guard_form_matches_fp64_in_higher_dimensions_and_with_classes(dim,
         assert O.uncovered_after_refinement(dim, [0.0] * dim, L, out[1][0], out[1][1], r, r, 40) == 0
 
 
+@pytest.mark.parametrize("dim,L,r", [(2, [1.0, 1.0], 0.01), (3, [1.0, 0.9, 1.1], 0.02), (5, [1.0] * 5, 0.15)])
+def test_extract_into_pinned_host_buffers(dim, L, r):
+    """rsagpu_domain_extract into pinned host buffers (written by the kernel across the link, no device staging)
+    gives the arrays of the staged path into ordinary (pageable) buffers, bit for bit."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    dom, algo = run_product(dim, L, r, 3)
+    pos, rad, ph = dom.arrays()
+    n = len(rad)
+    P = torch.empty((n + 7, dim), dtype=torch.float64, pin_memory=True).numpy()
+    R = torch.empty(n + 7, dtype=torch.float64, pin_memory=True).numpy()
+    H = torch.empty(n + 7, dtype=torch.int32, pin_memory=True).numpy()
+    k = C.c_uint64()
+    L_ = _lib.lib()
+    for out in ((P, R, H), (P, None, None), (None, R, H)):
+        for a in out:
+            if a is not None:
+                a.fill(-1)
+        args = [_lib.ptr(out[0], _lib._d) if out[0] is not None else None,
+                _lib.ptr(out[1], _lib._d) if out[1] is not None else None,
+                _lib.ptr(out[2], _lib._i32) if out[2] is not None else None]
+        _lib.check(L_.rsagpu_domain_extract(dom._h, *args, n + 7, C.byref(k)))
+        assert k.value == n
+        if out[0] is not None:
+            np.testing.assert_array_equal(out[0][:n], pos)
+            assert np.all(out[0][n:] == -1)  # nothing written past the spheres
+        if out[1] is not None:
+            np.testing.assert_array_equal(out[1][:n], rad)
+            np.testing.assert_array_equal(out[2][:n], ph)
+    algo.close()
+    dom.close()
+
+
 def test_class_overshoot_ends_the_class():
     """A capped round under the reference's pivot rule can keep more spheres than its class still wants (here the
     first round of the 0.004 class, in some of the seeds).  The product loop then ends the class and draws the
