@@ -61,9 +61,9 @@ int rsagpu_domain_spheres_volume(rsagpu_domain* dom, double* out);
 int rsagpu_domain_count(rsagpu_domain* dom, uint64_t* out);
 /* extract_spheres (rsa_grid.ixx:88-98): copies at most cap spheres into caller buffers
  * (centers: cap*dim doubles, row major; radii: cap; phases: cap; any may be NULL) in cell order,
- * and writes the number of spheres to *n_out.  Buffers in pinned host memory (cudaHostAlloc,
- * cudaHostRegister) are written by the device directly; others through a device copy.  The call returns
- * when the buffers hold the spheres. */
+ * and writes the number of spheres to *n_out.  Buffers in pinned host memory that the device addresses at
+ * the same pointer (cudaHostAlloc's, with unified addressing) are written by the device directly; others
+ * through a device copy.  The call returns when the buffers hold the spheres. */
 int rsagpu_domain_extract(rsagpu_domain* dom, double* centers, double* radii, int* phases,
                           uint64_t cap, uint64_t* n_out);
 /* operator_check_cell validators (operator_check_cell.ixx:8-78, rsa_data_storage.ixx:216-243):
