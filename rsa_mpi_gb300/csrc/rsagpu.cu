@@ -615,7 +615,9 @@ void begin(rsagpu_algo* A) {
     // twice the lattice: the list refilled at the second refinement (whose voxels outnumber the lattice's in 3D,
     // 1.5x at r = 0.002) then fits without a reallocation inside the run.  Growing it there cost a fresh mapping
     // of about 3 GB (2.5 ms with the GPU idle), as the memory pool had split the block of the previous run's size.
-    ensure_vox(A, 0, V, 2 * V);
+    // Lattices whose doubled list would pass 16 GB get no headroom.
+    const bool headroom = (double)V * (double)D * sizeof(int64_t) * 2.0 <= 16e9;
+    ensure_vox(A, 0, V, headroom ? 2 * V : V);
     A->cur = 0;
     A->V = V;
     A->level = 0;
