@@ -469,9 +469,10 @@ void ensure_cand(rsagpu_algo* A, uint64_t n) {
     if (n <= C.cap) return;
     uint32_t* keep = C.a.counters;
     C.a.counters = nullptr;
+    const uint64_t grown = C.cap + C.cap / 2;  // geometric growth: few reallocations in a run of growing rounds
     C.release();
     C.a.counters = keep;
-    const uint64_t cap = std::max<uint64_t>(n, 1024);
+    const uint64_t cap = std::max<uint64_t>({n, 1024, std::min<uint64_t>(grown, 0x7fffffffull)});
     if (cap > 0x7fffffffull) raise(RSAGPU_ERR_CAPACITY, "more than 2^31 candidates in one round");
     C.a.pos = dalloc<double>(cap * D);
     C.a.key = dalloc<uint64_t>(cap);
@@ -618,6 +619,13 @@ void begin(rsagpu_algo* A) {
     // Lattices whose doubled list would pass 16 GB get no headroom.
     const bool headroom = (double)V * (double)D * sizeof(int64_t) * 2.0 <= 16e9;
     ensure_vox(A, 0, V, headroom ? 2 * V : V);
+    // the candidate buffers of the run's rounds at once: rounds grow from the survivor-bounded first ones to the
+    // voxel-based size of the first refinements (about 0.37 darts per lattice voxel at config 2), and every growth
+    // reallocates 15 arrays, at the risk of a fresh mapping with the GPU idle
+    if (A->schedule != RSAGPU_SCHEDULE_REFERENCE) {
+        const double want = std::min(2.0 * A->factor * (double)V, (double)A->max_darts);
+        if (want * 256.0 <= 16e9) ensure_cand(A, (uint64_t)want);
+    }
     A->cur = 0;
     A->V = V;
     A->level = 0;
