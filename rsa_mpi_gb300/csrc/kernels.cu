@@ -613,13 +613,13 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
             if (load_state(c.state, i) == ST_UNDECIDED) {
                 bool any_acc = false, all_rej = true;
                 const uint8_t nb = c.nblk[i];
-                auto judge = [&](int32_t j) {
+                auto tally_blocker = [&](int32_t j) {
                     const uint8_t s = load_state(c.state, j);
                     any_acc |= (s == ST_ACCEPTED);
                     all_rej &= (s == ST_REJECTED);
                 };
                 if (nb != NB_OVERFLOW) {
-                    for (int b = 0; b < nb; b++) judge(blk_index(c.blk[(uint64_t)i * NB + b]));
+                    for (int b = 0; b < nb; b++) tally_blocker(blk_index(c.blk[(uint64_t)i * NB + b]));
                 } else {
                     double x[D];
 #pragma unroll
@@ -631,7 +631,7 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
                         cell_of<D>(g, geo, x, k);
                         visit_candidates(g, geo, c, k, nullptr, search_r2(r, cand_rmax(g, c)), [&](int32_t j, const double* img, const int8_t*) {
                             if (!precedes(c.key[j], j, key, i)) return false;
-                            if (collide64<D>(r, x, c.rad[j], img)) judge(j);
+                            if (collide64<D>(r, x, c.rad[j], img)) tally_blocker(j);
                             return any_acc;
                         });
                     } else {
@@ -646,7 +646,7 @@ __device__ __forceinline__ bool settle_body(const Grid<D>& g, const Geo<D>& geo,
         asm volatile("" : "+f"(rf));  // not rematerialised in the loop below: the conversion runs on the FP64 pipe
                         visit_candidates_o(g, c, k, offq, search_r2f(rf, cand_rmaxf(g, c)), [&](int32_t j, const int32_t* o, const int8_t* q) {
                             if (!precedes(c.key[j], j, key, i)) return false;
-                            if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) judge(j);
+                            if (cand_collide32(g, geo, c, x, r, offq, rf, j, o, q, rt)) tally_blocker(j);
                             return any_acc;
                         });
                     }
